@@ -1,0 +1,327 @@
+"""Seeded synthetic initial data for the five benchmark workloads.
+
+The reference's regression drivers build initial data by evaluating an
+``InitialDataFunction`` at cell centres (``MeshOperator::generate``,
+src/MeshOperator.cpp:168-189) and, for magnetised problems, by turning a
+face-centred vector potential into a divergence-free cell field
+(src/Problems.cpp:660-667).  These generators do the same in numpy, in the
+reference's AoS layout ``(ni+2g, nj+2g, nk+2g, nq)`` with guards filled by
+the boundary condition, so one array feeds the GPU solver and the CPU oracle
+identically.
+
+Randomness comes from SplitMix64 (Steele, Lea & Flood 2014) so that every
+machine produces the same bits.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .scheme import Scheme
+
+MASK64 = (1 << 64) - 1
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n successive SplitMix64 outputs as uint64."""
+    out = np.empty(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        z = np.uint64(seed & MASK64) + idx * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        out[:] = z ^ (z >> np.uint64(31))
+    return out
+
+
+def uniform(seed: int, n: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+    """n doubles uniform in [lo, hi) from the top 53 bits of SplitMix64."""
+    u = (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return lo + (hi - lo) * u
+
+
+def cell_centres(s: Scheme):
+    """Cell-centre coordinates of every cell including guards
+    (CartesianMeshGeometry::coordinateAtIndex, lower + dx * (i + 0.5))."""
+    out = []
+    for a in range(3):
+        n, g = s.shape[a], s.ng[a]
+        dx = (s.upper[a] - s.lower[a]) / n
+        idx = np.arange(-g, n + g, dtype=np.float64)
+        out.append(s.lower[a] + dx * (idx + 0.5))
+    return np.meshgrid(*out, indexing="ij")
+
+
+def apply_bc_numpy(s: Scheme, P: np.ndarray) -> np.ndarray:
+    """Guard fill of BoundaryCondition::applySimple (src/BoundaryConditions.cpp:
+    8-176): axis by axis, left then right, over the full transverse extent."""
+    for a in range(3):
+        g = s.ng[a]
+        if g == 0:
+            continue
+        N = P.shape[a]
+        P = np.moveaxis(P, a, 0)
+        for n in range(g):
+            if s.bc == "periodic":
+                P[n] = P[N - 2 * g + n]
+            elif s.bc == "outflow":
+                P[n] = P[g]
+            else:
+                P[n] = P[2 * g - n - 1]
+                P[n, ..., 1 + a] *= -1
+        for n in range(g):
+            if s.bc == "periodic":
+                P[N - g + n] = P[g + n]
+            elif s.bc == "outflow":
+                P[N - n - 1] = P[N - g - 1]
+            else:
+                P[N - n - 1] = P[N - 2 * g + n]
+                P[N - n - 1, ..., 1 + a] *= -1
+        P = np.moveaxis(P, 0, a)
+    return P
+
+
+def empty_state(s: Scheme) -> np.ndarray:
+    return np.zeros(s.full_shape, dtype=np.float64)
+
+
+# ----------------------------------------------------------------------------
+# workload 1: Sod shock tube (src/Problems.cpp:37-42 states)
+# ----------------------------------------------------------------------------
+def sod(n: int = 1024, gamma: float = 1.4):
+    s = Scheme(law="hydro", recon="plm", riemann="hlle", bc="outflow", rk_order=2,
+               shape=(n, 1, 1), gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+    P = empty_state(s)
+    x, _, _ = cell_centres(s)
+    left = x < 0.5
+    P[..., 0] = np.where(left, 1.0, 0.125)
+    P[..., 4] = np.where(left, 1.0, 0.1)
+    return s, apply_bc_numpy(s, P)
+
+
+# ----------------------------------------------------------------------------
+# workload 2: Kelvin-Helmholtz, periodic [0,1]^2
+# ----------------------------------------------------------------------------
+KH_SEED = 20261203
+
+
+def kelvin_helmholtz(n: int = 1024, seed: int = KH_SEED, riemann: str = "hllc"):
+    s = Scheme(law="hydro", recon="plm", riemann=riemann, bc="periodic", rk_order=2,
+               shape=(n, n, 1), gamma=5.0 / 3, plm_theta=1.5, cfl=0.4, t_final=1.0)
+    P = empty_state(s)
+    g = s.ng[0]
+    _, y, _ = cell_centres(s)
+    band = np.abs(y - 0.5) < 0.25
+    P[..., 0] = np.where(band, 2.0, 1.0)
+    P[..., 1] = np.where(band, 0.5, -0.5)
+    P[..., 4] = 2.5
+    vy = uniform(seed, n * n, -1.0, 1.0).reshape(n, n) * 0.01
+    P[g:g + n, g:g + n, 0, 2] = vy
+    return s, apply_bc_numpy(s, P)
+
+
+# ----------------------------------------------------------------------------
+# workload 3: 3-D Newtonian MHD turbulence with a vector-potential B field
+# ----------------------------------------------------------------------------
+MHD_SEED = 314159
+
+
+def _fourier_modes(seed: int, kmax: int = 4):
+    ks = [(a, b, c) for a in range(-kmax, kmax + 1) for b in range(-kmax, kmax + 1)
+          for c in range(-kmax, kmax + 1) if 0 < a * a + b * b + c * c <= kmax * kmax]
+    r = uniform(seed, 4 * len(ks)).reshape(len(ks), 4)
+    return np.array(ks, dtype=np.float64), r
+
+
+def _fourier_vector(seed, X, Y, Z, kmax=4):
+    """Sum over modes 0 < |k| <= kmax of a random-amplitude, random-phase
+    vector wave; returns (3, *X.shape)."""
+    ks, r = _fourier_modes(seed, kmax)
+    out = np.zeros((3,) + X.shape)
+    for m, k in enumerate(ks):
+        phase = 2 * math.pi * (k[0] * X + k[1] * Y + k[2] * Z) + 2 * math.pi * r[m, 3]
+        amp = (r[m, :3] - 0.5) / max(1.0, float(np.dot(k, k)))
+        out += amp[:, None, None, None] * np.cos(phase)[None]
+    return out
+
+
+def vector_potential_to_cell_b(s: Scheme, A: np.ndarray) -> np.ndarray:
+    """B = divergence(CT(fluxes of A)) on every cell including guards, as in
+    src/Problems.cpp:660-667 with CellCenteredFieldCT::vectorPotentialToFluxes
+    (src/CellCenteredFieldCT.cpp:136-150), the flux CT stencil (:14-134) and
+    MeshOperator::divergence with factor 1 (src/MeshOperator.cpp:323-381).
+    A has shape (N0+1, N1+1, N2+1, 3, 3): component, face axis."""
+    F = np.zeros_like(A)
+    F[..., 1, 0] = -A[..., 2, 0]
+    F[..., 2, 0] = +A[..., 1, 0]
+    F[..., 2, 1] = -A[..., 0, 1]
+    F[..., 0, 1] = +A[..., 2, 1]
+    F[..., 0, 2] = -A[..., 1, 2]
+    F[..., 1, 2] = +A[..., 0, 2]
+    G = ct_correct_numpy(F, 0)
+    dx = [(s.upper[a] - s.lower[a]) / s.shape[a] for a in range(3)]
+    dA = [dx[1] * dx[2], dx[2] * dx[0], dx[0] * dx[1]]
+    dV = dx[0] * dx[1] * dx[2]
+    n0, n1, n2 = A.shape[0] - 1, A.shape[1] - 1, A.shape[2] - 1
+    B = (1.0 / dV) * (
+        + G[1:, :n1, :n2, :, 0] * dA[0] - G[:n0, :n1, :n2, :, 0] * dA[0]
+        + G[:n0, 1:, :n2, :, 1] * dA[1] - G[:n0, :n1, :n2, :, 1] * dA[1]
+        + G[:n0, :n1, 1:, :, 2] * dA[2] - G[:n0, :n1, :n2, :, 2] * dA[2])
+    return B
+
+
+def ct_correct_numpy(F: np.ndarray, ib: int) -> np.ndarray:
+    """CellCenteredFieldCT::correctGodunovFluxes (src/CellCenteredFieldCT.cpp:
+    14-134), Toth (2000) eq. 25, vectorised."""
+    G = F.copy()
+    n0, n1, n2 = F.shape[:3]
+    B0, B1, B2 = ib, ib + 1, ib + 2
+    G[..., B0, 0] = 0.0
+    G[..., B1, 1] = 0.0
+    G[..., B2, 2] = 0.0
+    f = F
+    if n0 >= 3:
+        if n1 >= 3:
+            G[1:, 1:-1, :, B1, 0] = 0.125 * (
+                + 2 * f[1:, 1:-1, :, B1, 0] + f[1:, 2:, :, B1, 0] + f[1:, :-2, :, B1, 0]
+                - f[1:, 2:, :, B0, 1] - f[:-1, 2:, :, B0, 1] - f[1:, 1:-1, :, B0, 1] - f[:-1, 1:-1, :, B0, 1])
+        if n2 >= 3:
+            G[1:, :, 1:-1, B2, 0] = 0.125 * (
+                + 2 * f[1:, :, 1:-1, B2, 0] + f[1:, :, 2:, B2, 0] + f[1:, :, :-2, B2, 0]
+                - f[1:, :, 2:, B0, 2] - f[:-1, :, 2:, B0, 2] - f[1:, :, 1:-1, B0, 2] - f[:-1, :, 1:-1, B0, 2])
+    if n1 >= 3:
+        if n2 >= 3:
+            G[:, 1:, 1:-1, B2, 1] = 0.125 * (
+                + 2 * f[:, 1:, 1:-1, B2, 1] + f[:, 1:, 2:, B2, 1] + f[:, 1:, :-2, B2, 1]
+                - f[:, 1:, 2:, B1, 2] - f[:, :-1, 2:, B1, 2] - f[:, 1:, 1:-1, B1, 2] - f[:, :-1, 1:-1, B1, 2])
+        if n0 >= 3:
+            G[1:-1, 1:, :, B0, 1] = 0.125 * (
+                + 2 * f[1:-1, 1:, :, B0, 1] + f[2:, 1:, :, B0, 1] + f[:-2, 1:, :, B0, 1]
+                - f[2:, 1:, :, B1, 0] - f[2:, :-1, :, B1, 0] - f[1:-1, 1:, :, B1, 0] - f[1:-1, :-1, :, B1, 0])
+    if n2 >= 3:
+        if n0 >= 3:
+            G[1:-1, :, 1:, B0, 2] = 0.125 * (
+                + 2 * f[1:-1, :, 1:, B0, 2] + f[2:, :, 1:, B0, 2] + f[:-2, :, 1:, B0, 2]
+                - f[2:, :, 1:, B2, 0] - f[2:, :, :-1, B2, 0] - f[1:-1, :, 1:, B2, 0] - f[1:-1, :, :-1, B2, 0])
+        if n1 >= 3:
+            G[:, 1:-1, 1:, B1, 2] = 0.125 * (
+                + 2 * f[:, 1:-1, 1:, B1, 2] + f[:, 2:, 1:, B1, 2] + f[:, :-2, 1:, B1, 2]
+                - f[:, 2:, 1:, B2, 1] - f[:, 2:, :-1, B2, 1] - f[:, 1:-1, 1:, B2, 1] - f[:, 1:-1, :-1, B2, 1])
+    return G
+
+
+def face_vector_potential(s: Scheme, fn) -> np.ndarray:
+    """MeshOperator::generate(face, scalars, boundaryShape) (src/MeshOperator.
+    cpp:119-167): fn(x, y, z) -> (3, ...) evaluated at the three face centres of
+    every index of the guard-extended mesh plus one."""
+    N = [s.shape[a] + 2 * s.ng[a] for a in range(3)]
+    dx = [(s.upper[a] - s.lower[a]) / s.shape[a] for a in range(3)]
+    idx = [np.arange(N[a] + 1, dtype=np.float64) - s.ng[a] for a in range(3)]
+    A = np.zeros((N[0] + 1, N[1] + 1, N[2] + 1, 3, 3))
+    for face in range(3):
+        c = []
+        for a in range(3):
+            off = -0.5 if a == face else 0.0
+            c.append(s.lower[a] + dx[a] * (idx[a] + off + 0.5))
+        X, Y, Z = np.meshgrid(*c, indexing="ij")
+        A[..., :, face] = np.moveaxis(fn(X, Y, Z), 0, -1)
+    return A
+
+
+def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms: float = 0.5,
+                   rk_order: int = 3):
+    s = Scheme(law="mhd", recon="plm", riemann="hlle", bc="periodic", rk_order=rk_order,
+               shape=(n, n, n), gamma=5.0 / 3, plm_theta=1.5, cfl=0.3, t_final=None, steps=100)
+    P = empty_state(s)
+    X, Y, Z = cell_centres(s)
+    v = _fourier_vector(seed, X, Y, Z)
+    g = s.ng[0]
+    inner = v[:, g:-g, g:-g, g:-g]
+    v *= v_rms / math.sqrt(float(np.mean(np.sum(inner ** 2, axis=0))))
+    P[..., 0] = 1.0
+    P[..., 4] = 1.0
+    P[..., 1:4] = np.moveaxis(v, 0, -1)
+    A = face_vector_potential(s, lambda x, y, z: _fourier_vector(seed + 1, x, y, z))
+    B = vector_potential_to_cell_b(s, A)
+    inner_b = B[g:-g, g:-g, g:-g]
+    scale = b_rms / math.sqrt(float(np.mean(np.sum(inner_b ** 2, axis=-1))))
+    P[..., 5:8] = B * scale
+    return s, apply_bc_numpy(s, P)
+
+
+# ----------------------------------------------------------------------------
+# workload 4: relativistic MHD cylindrical blast wave on [-6, 6]^2
+# ----------------------------------------------------------------------------
+def rmhd_blast(n: int = 512, pressure_floor: float = -1.0):
+    s = Scheme(law="rmhd", recon="weno5", riemann="hlle", bc="outflow", rk_order=3,
+               shape=(n, n, 1), lower=(-6.0, -6.0, 0.0), upper=(6.0, 6.0, 1.0), gamma=4.0 / 3,
+               cfl=0.3, t_final=4.0, pressure_floor=pressure_floor)
+    P = empty_state(s)
+    x, y, _ = cell_centres(s)
+    r = np.sqrt(x * x + y * y)
+    P[..., 0] = 0.01
+    P[..., 4] = np.where(r < 0.8, 1.0, 0.01)
+    P[..., 5] = 0.1
+    return s, apply_bc_numpy(s, P)
+
+
+# ----------------------------------------------------------------------------
+# workload 5: stream of Riemann problems of uneven sizes
+# ----------------------------------------------------------------------------
+RIEMANN_SEED = 27182818
+
+
+@dataclass
+class RiemannRequest:
+    index: int
+    arrival: float
+    dims: int
+    n: int
+    theta: float
+    left: tuple
+    right: tuple
+    scheme: Scheme = field(repr=False, default=None)
+
+    def zones(self) -> int:
+        return self.n ** self.dims
+
+
+def riemann_stream(count: int = 4096, rate: float = 2000.0, seed: int = RIEMANN_SEED,
+                   n1=(256, 8192), n2=(128, 512)):
+    """Seeded Poisson arrivals (rate per second) of 1-D / 2-D Riemann problems.
+    Half are 1-D with N log-uniform in n1, half 2-D with side log-uniform in n2;
+    rho log-uniform in [0.1, 10], p in [0.01, 100], velocities uniform in
+    [-1, 1]; the 2-D interface passes through the centre at a random angle."""
+    r = uniform(seed, count * 16).reshape(count, 16)
+    out, t = [], 0.0
+    for m in range(count):
+        t += -math.log(1.0 - r[m, 0]) / rate
+        dims = 1 if r[m, 1] < 0.5 else 2
+        lo, hi = (n1 if dims == 1 else n2)
+        nn = int(round(math.exp(math.log(lo) + (math.log(hi) - math.log(lo)) * r[m, 2])))
+        def logu(u, a, b):
+            return math.exp(math.log(a) + (math.log(b) - math.log(a)) * u)
+        left = (logu(r[m, 3], 0.1, 10), 2 * r[m, 4] - 1, (2 * r[m, 5] - 1) if dims == 2 else 0.0, 0.0,
+                logu(r[m, 6], 0.01, 100))
+        right = (logu(r[m, 7], 0.1, 10), 2 * r[m, 8] - 1, (2 * r[m, 9] - 1) if dims == 2 else 0.0, 0.0,
+                 logu(r[m, 10], 0.01, 100))
+        theta = 2 * math.pi * r[m, 11]
+        out.append(RiemannRequest(m, t, dims, nn, theta, left, right))
+    return out
+
+
+def riemann_initial(req: RiemannRequest, gamma: float = 5.0 / 3):
+    shape = (req.n, 1, 1) if req.dims == 1 else (req.n, req.n, 1)
+    s = Scheme(law="hydro", recon="plm", riemann="hllc", bc="outflow", rk_order=2, shape=shape,
+               gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+    P = empty_state(s)
+    x, y, _ = cell_centres(s)
+    if req.dims == 1:
+        side = (x - 0.5) < 0
+    else:
+        side = (x - 0.5) * math.cos(req.theta) + (y - 0.5) * math.sin(req.theta) < 0
+    for q in range(5):
+        P[..., q] = np.where(side, req.left[q], req.right[q])
+    return s, apply_bc_numpy(s, P)
