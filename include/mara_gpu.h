@@ -1,0 +1,154 @@
+/*
+ * mara_gpu.h -- C ABI of the GB300-native Mara2 finite-volume time step.
+ *
+ * The drop-in boundary is Mara2's SolutionScheme interface
+ * (src/Mara.hpp:87-97): a GPU MethodOfLinesTVD whose advance() mutates
+ * MeshData::P in place, plus the separate FieldOperator::getCourantTimestep
+ * call that drivers make for dt (src/FieldOperator.hpp:80).  Every entry
+ * point takes plain pointers and sizes, returns an int status (0 = success)
+ * and never throws; the C++ wrapper in mara2_gb300/csrc/GpuSolutionScheme.hpp
+ * turns statuses back into the reference's exception types.
+ *
+ * Array layout at the boundary is the reference's MeshData::P: FP64 AoS
+ * (ni+2g0, nj+2g1, nk+2g2, nq) in C order, q fastest, guard zones only on
+ * axes with more than one interior cell (src/MeshData.cpp:8-28).  On the
+ * device the state is kept structure-of-arrays with x fastest.
+ *
+ * A handle owns one CUDA stream and its device memory; it is not
+ * thread-safe.  Calls on one handle are ordered on its stream.
+ */
+#ifndef MARA_GPU_H
+#define MARA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ConservationLaw subclasses: NewtonianHydro, NewtonianMHD, RelativisticMHD
+ * (src/ConservationLaws.hpp:25-100) */
+enum { MARA_LAW_HYDRO = 0, MARA_LAW_MHD = 1, MARA_LAW_RMHD = 2 };
+/* IntercellFluxScheme: MethodOfLines (PCM), MethodOfLinesPlm, and the WENO5
+ * primitive-reconstruction composition (src/IntercellFluxSchemes.hpp) */
+enum { MARA_RECON_PCM = 0, MARA_RECON_PLM = 1, MARA_RECON_WENO5 = 2 };
+/* RiemannSolver: HlleRiemannSolver, HllcNewtonianHydroRiemannSolver
+ * (src/RiemannSolvers.hpp:27-50) */
+enum { MARA_RIEMANN_HLLE = 0, MARA_RIEMANN_HLLC = 1 };
+/* BoundaryCondition: Periodic, Outflow, Reflecting (src/BoundaryConditions.hpp) */
+enum { MARA_BC_PERIODIC = 0, MARA_BC_OUTFLOW = 1, MARA_BC_REFLECTING = 2 };
+/* Reconstruction::SmoothnessIndicator (src/Reconstruction.hpp) */
+enum { MARA_WENO_JS96 = 0, MARA_WENO_BORGES08 = 1, MARA_WENO_SHENZHA10 = 2 };
+/* arithmetic of the step */
+enum {
+    MARA_PRECISION_FP64 = 0,  /* plain: matches the reference's FP64 CPU path  */
+    MARA_PRECISION_MIXED = 1  /* FP32 reconstruction/Riemann/flux arithmetic,
+                                 compensated FP32 pair (hi+lo) conserved-state
+                                 accumulator, FP64 RMHD Newton iteration      */
+};
+
+/* Status codes.  1..8 mirror ConsToPrimRMHD's enum (src/ConsToPrimRMHD.hpp:
+ * 9-20); 16..20 name the exceptions the reference throws on this path. */
+enum {
+    MARA_OK = 0,
+    MARA_C2P_CONS_CONTAINS_NAN = 1,
+    MARA_C2P_CONS_NEGATIVE_DENSITY = 2,
+    MARA_C2P_CONS_NEGATIVE_ENERGY = 3,
+    MARA_C2P_PRIM_CONTAINS_NAN = 4,
+    MARA_C2P_PRIM_NEGATIVE_PRESSURE = 5,
+    MARA_C2P_PRIM_NEGATIVE_RESTMASS = 6,
+    MARA_C2P_PRIM_SUPERLUMINAL = 7,
+    MARA_C2P_MAXITER = 8,
+    MARA_ERR_INVERSION_FAILURE = 16, /* FieldOperator::InversionFailure       */
+    MARA_ERR_SUPERLUMINAL = 17,      /* std::runtime_error, superluminal      */
+    MARA_ERR_BAD_EIGENVALUES = 18,   /* std::runtime_error, bad eigenvalues   */
+    MARA_ERR_GUARD_TOO_SMALL = 19,   /* std::logic_error from makeFootprint   */
+    MARA_ERR_CONFIG = 20,            /* std::logic_error, bad configuration   */
+    MARA_ERR_CUDA = 32,              /* a CUDA runtime call failed            */
+    MARA_ERR_NO_DEVICE = 33,
+    MARA_ERR_ARGUMENT = 34,
+    MARA_ERR_TOO_LARGE = 35
+};
+
+typedef struct MaraGpuConfig {
+    int law, recon, riemann, bc;
+    int rk_order;        /* MethodOfLinesTVD::setRungeKuttaOrder: 1, 2, 3     */
+    int disable_ct;      /* MethodOfLinesTVD::setDisableFieldCT              */
+    int weno_is;         /* MARA_WENO_*                                      */
+    int ni, nj, nk;      /* interior cells (CartesianMeshGeometry cellsShape) */
+    int ng[3];           /* guard zones per axis (MeshData boundaryShape)     */
+    double lower[3], upper[3];   /* CartesianMeshGeometry::setLowerUpper     */
+    double gamma;        /* ConservationLaw::setGammaLawIndex                */
+    double plm_theta;    /* IntercellFluxScheme::setPlmTheta                 */
+    double shenzha_A;    /* Reconstruction::setShenZha10A                    */
+    double pressure_floor; /* ConservationLaw::setPressureFloor              */
+    int precision;       /* MARA_PRECISION_*                                 */
+    int device;          /* CUDA device ordinal                              */
+} MaraGpuConfig;
+
+typedef struct MaraGpuStats {
+    int status;          /* status of the last advance                       */
+    int failures;        /* zones whose primitive recovery failed            */
+    int first_zone[3];   /* interior-relative index of the lowest failed zone */
+    int first_code;      /* status of that zone                              */
+    int64_t steps;       /* advances done on this handle                     */
+    int64_t kernel_launches; /* kernels this handle has launched             */
+    double last_dt;
+} MaraGpuStats;
+
+typedef struct MaraGpuHandle MaraGpuHandle;
+
+/* Replaces the construction of MethodOfLinesTVD + its injected operators
+ * (SolutionSchemes.hpp:49-72, Mara.hpp:44-51).  Validates the configuration
+ * like SchemeHelpers::makeFootprint (SolutionSchemes.cpp:17-49). */
+int mara_gpu_create(const MaraGpuConfig* config, MaraGpuHandle** handle);
+int mara_gpu_destroy(MaraGpuHandle* handle);
+
+/* Host <-> device copies of MeshData::P (with guards, AoS FP64). */
+int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos);
+int mara_gpu_download(MaraGpuHandle* h, double* P_aos);
+
+/* MethodOfLinesTVD::advance (SolutionSchemes.cpp:108-275) on the resident
+ * state: every RK stage, flux CT when the law is magnetic, primitive recovery
+ * and the guard fill.  Asynchronous; the status of earlier steps is reported
+ * by the next synchronising call. */
+int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt);
+
+/* The drop-in form of advance: P_aos (host) in, advanced P_aos out, as
+ * SolutionScheme::advance(MeshData&, t0, dt) does on MeshData::P.  Copies in,
+ * advances, copies back and synchronises. */
+int mara_gpu_advance_host(MaraGpuHandle* h, double* P_aos, double t0, double dt);
+
+/* FieldOperator::getCourantTimestep (FieldOperator.cpp:125-169) with
+ * L = MeshOperator::linearCellDimension, on the resident state (without the
+ * driver's CFL factor).  Synchronises. */
+int mara_gpu_courant(MaraGpuHandle* h, double* dt);
+
+/* Device-resident driver loop (the regression drivers' timestep/advance
+ * pair, src/Problems.cpp:181-188): up to max_steps steps of
+ * dt = min(cfl * courant, t_final - t) while t < t_final (t_final < 0 means
+ * no end time).  dt never leaves the device.  *t is read and updated. */
+int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, double* t, int* steps_done);
+
+/* Wait for the handle's stream; returns the first error seen. */
+int mara_gpu_synchronize(MaraGpuHandle* h);
+int mara_gpu_stats(MaraGpuHandle* h, MaraGpuStats* stats);
+
+/* The handle's cudaStream_t, for callers that time or order work on it. */
+void* mara_gpu_stream(MaraGpuHandle* h);
+
+/* Optional per-kernel timing with CUDA events around each launch of the
+ * stage kernels (off by default).  ms_total/launches are per kernel class:
+ * [0] flux / stage kernels, [1] update, [2] courant. */
+int mara_gpu_set_kernel_timing(MaraGpuHandle* h, int enable);
+int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches[3]);
+
+/* Device bytes the handle holds. */
+int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
+
+const char* mara_gpu_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,65 @@
+// internal.h -- declarations shared by the CUDA translation units of the
+// library (not part of the public C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mara {
+
+// Mesh description passed by value to every kernel.  Device arrays are
+// structure-of-arrays with x fastest:
+//   P (with guards)   P[q * sP + (k * N1 + j) * N0 + i]
+//   U (interior only) U[q * sU + (k * n1 + j) * n0 + i]
+//   F_a (face fluxes) F[q * sF + (k * (N1+1) + j) * (N0+1) + i], face i is
+//                     the left face of cell i along axis a
+struct GridDesc {
+    int n[3];          // interior cells
+    int g[3];          // guard cells (0 on flat axes)
+    int N[3];          // n + 2 g
+    long long sP, sU, sF;
+    double nrm[3][3];  // face normals exactly as the reference builds them
+    double dA[3], dV;  // CartesianMeshGeometry face areas and volume
+    double lmin;       // MeshOperator::linearCellDimension
+    int bc;
+    int ct;            // flux CT on the magnetic fluxes
+    int nq;
+};
+
+// Device-side status of a handle: the first error and the inversion-failure
+// bookkeeping of FieldOperator::recoverPrimitive.
+struct DevStatus {
+    int code;                       // first non-zero status (0 = ok)
+    int failures;                   // zones whose recovery failed
+    int first_code;                 // status of the lowest failed zone
+    int done;                       // driver loop reached t_final
+    unsigned long long first_zone;  // lowest failed interior zone, linear
+    unsigned long long dt_bits;     // Courant reduction (min of positive doubles)
+    double t;                       // driver-loop time
+    double dt;                      // dt of the current step
+    long long steps;                // driver-loop steps taken
+};
+
+struct PhysParamsH {
+    double gamma, plm_theta, shenzha_A, pressure_floor;
+    int weno_is;
+};
+
+// ---- plain FP64 path (plain_fp64.cu) -----------------------------------------
+void plain_flux(int law, int recon, int riemann, int axis, const GridDesc& G, const PhysParamsH& pp,
+                const double* P, double* F, DevStatus* st, cudaStream_t s);
+void plain_update(int law, const GridDesc& G, const PhysParamsH& pp, const double* Pin, double* Pout,
+                  double* U0, double* U, const double* Fx, const double* Fy, const double* Fz,
+                  double b, int stage, const double* dt, DevStatus* st, cudaStream_t s);
+void plain_courant(int law, const GridDesc& G, const PhysParamsH& pp, const double* P, DevStatus* st,
+                   cudaStream_t s);
+
+// ---- shared helpers (mara_gpu.cu) --------------------------------------------
+void launch_courant_init(DevStatus* st, cudaStream_t s);
+void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s);
+void launch_set_dt(DevStatus* st, double dt, cudaStream_t s);
+void launch_advance_time(DevStatus* st, cudaStream_t s);
+void launch_aos_to_soa(const double* aos, double* soa, const GridDesc& G, cudaStream_t s);
+void launch_soa_to_aos(const double* soa, double* aos, const GridDesc& G, cudaStream_t s);
+
+} // namespace mara

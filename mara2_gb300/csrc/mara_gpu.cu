@@ -1,0 +1,584 @@
+// mara_gpu.cu -- the C ABI (include/mara_gpu.h): handle life cycle, layout
+// transposes between the reference's AoS MeshData::P and the device SoA
+// state, the RK stage sequence of MethodOfLinesTVD::advance, the device-side
+// driver loop and its CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/mara_gpu.h"
+#include "internal.h"
+#include "mixed.h"
+
+using namespace mara;
+
+namespace mara {
+
+// ---------------------------------------------------------------------------
+// small device helpers
+__global__ void k_courant_init(DevStatus* st)
+{
+    const double big = DBL_MAX;
+    st->dt_bits = (unsigned long long) __double_as_longlong(big);
+}
+
+// dt = min(cfl * courant, t_final - t) as the regression drivers compute it
+// (src/Problems.cpp:181-186); a step at t >= t_final is not taken.
+__global__ void k_dt_from_courant(DevStatus* st, double cfl, double t_final)
+{
+    if (st->done) return;
+    const double courant = __longlong_as_double((long long) st->dt_bits);
+    double dt = cfl * courant;
+    if (t_final >= 0.0) {
+        if (!(st->t < t_final)) { st->done = 1; return; }
+        const double dt2 = t_final - st->t;
+        dt = dt < dt2 ? dt : dt2;
+    }
+    st->dt = dt;
+}
+
+__global__ void k_set_dt(DevStatus* st, double dt) { st->dt = dt; }
+
+__global__ void k_advance_time(DevStatus* st)
+{
+    if (st->done || st->code) return;
+    st->t += st->dt;
+    st->steps += 1;
+}
+
+__global__ void k_run_begin(DevStatus* st, double t)
+{
+    st->t = t;
+    st->steps = 0;
+    st->done = 0;
+}
+
+// AoS (i, j, k, q), q fastest  <->  SoA q * sP + (k * N1 + j) * N0 + i
+__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, GridDesc G)
+{
+    const long long cells = G.sP;
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; // AoS cell order
+    if (c >= cells) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    for (int q = 0; q < G.nq; ++q) soa[q * G.sP + s] = aos[c * G.nq + q];
+}
+
+__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos, GridDesc G)
+{
+    const long long cells = G.sP;
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    for (int q = 0; q < G.nq; ++q) aos[c * G.nq + q] = soa[q * G.sP + s];
+}
+
+void launch_courant_init(DevStatus* st, cudaStream_t s) { k_courant_init<<<1, 1, 0, s>>>(st); }
+void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s)
+{
+    k_dt_from_courant<<<1, 1, 0, s>>>(st, cfl, t_final);
+}
+void launch_set_dt(DevStatus* st, double dt, cudaStream_t s) { k_set_dt<<<1, 1, 0, s>>>(st, dt); }
+void launch_advance_time(DevStatus* st, cudaStream_t s) { k_advance_time<<<1, 1, 0, s>>>(st); }
+void launch_aos_to_soa(const double* aos, double* soa, const GridDesc& G, cudaStream_t s)
+{
+    const long long n = G.sP;
+    k_aos_to_soa<<<(unsigned) ((n + 255) / 256), 256, 0, s>>>(aos, soa, G);
+}
+void launch_soa_to_aos(const double* soa, double* aos, const GridDesc& G, cudaStream_t s)
+{
+    const long long n = G.sP;
+    k_soa_to_aos<<<(unsigned) ((n + 255) / 256), 256, 0, s>>>(soa, aos, G);
+}
+
+} // namespace mara
+
+// ---------------------------------------------------------------------------
+struct TimedPair {
+    cudaEvent_t a, b;
+    int cls;
+};
+
+struct MaraGpuHandle {
+    MaraGpuConfig cfg;
+    GridDesc G;
+    PhysParamsH pp;
+    cudaStream_t stream = nullptr;
+    double* P[2] = {nullptr, nullptr};  // primitive state with guards (plain path)
+    int cur = 0;
+    double* U0 = nullptr;
+    double* U = nullptr;
+    double* F[3] = {nullptr, nullptr, nullptr};
+    double* stage_aos = nullptr;         // device AoS staging for transposes
+    DevStatus* st = nullptr;
+    DevStatus* st_host = nullptr;        // pinned mirror
+    MixedState* mixed = nullptr;         // mixed-precision path
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    double graph_cfl = -1.0, graph_tfinal = -2.0;
+    int64_t steps = 0, launches = 0;
+    int64_t bytes = 0;
+    int timing = 0;
+    std::vector<TimedPair> timed;
+    double ms_total[3] = {0, 0, 0};
+    int64_t timed_launches[3] = {0, 0, 0};
+    int last_status = 0;
+    MaraGpuStats last_stats;
+};
+
+static int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return MARA_OK;
+    std::fprintf(stderr, "mara_gpu: CUDA error: %s\n", cudaGetErrorString(e));
+    return MARA_ERR_CUDA;
+}
+
+#define CK(call) do { const cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_status(e_); } while (0)
+
+static int alloc(MaraGpuHandle* h, void** p, size_t bytes)
+{
+    CK(cudaMalloc(p, bytes));
+    CK(cudaMemsetAsync(*p, 0, bytes, h->stream));
+    h->bytes += (int64_t) bytes;
+    return MARA_OK;
+}
+
+static void timed_begin(MaraGpuHandle* h, int cls, TimedPair& tp)
+{
+    tp.cls = cls;
+    if (!h->timing) return;
+    cudaEventCreate(&tp.a);
+    cudaEventCreate(&tp.b);
+    cudaEventRecord(tp.a, h->stream);
+}
+
+static void timed_end(MaraGpuHandle* h, TimedPair& tp)
+{
+    if (!h->timing) return;
+    cudaEventRecord(tp.b, h->stream);
+    h->timed.push_back(tp);
+}
+
+static int validate(const MaraGpuConfig* c)
+{
+    const int n[3] = {c->ni, c->nj, c->nk};
+    const int s = c->recon == MARA_RECON_PCM ? 1 : c->recon == MARA_RECON_PLM ? 2 : c->recon == MARA_RECON_WENO5 ? 3 : 0;
+    if (c->law < 0 || c->law > 2 || s == 0 || c->riemann < 0 || c->riemann > 1 || c->bc < 0 || c->bc > 2)
+        return MARA_ERR_CONFIG;
+    if (c->rk_order < 1 || c->rk_order > 3) return MARA_ERR_CONFIG;
+    if (c->precision != MARA_PRECISION_FP64 && c->precision != MARA_PRECISION_MIXED) return MARA_ERR_CONFIG;
+    for (int a = 0; a < 3; ++a) {
+        if (n[a] < 1 || c->ng[a] < 0) return MARA_ERR_CONFIG;
+        if (n[a] == 1 && c->ng[a] != 0) return MARA_ERR_CONFIG;
+        if (n[a] > 1 && c->ng[a] < s) return MARA_ERR_GUARD_TOO_SMALL;
+        if (n[a] > 1 && n[a] < 2 * c->ng[a]) return MARA_ERR_CONFIG; // guards are images of interior zones
+        if (n[a] > 65535 && a > 0) return MARA_ERR_TOO_LARGE;
+    }
+    if (c->upper[0] <= c->lower[0] || c->upper[1] <= c->lower[1] || c->upper[2] <= c->lower[2])
+        return MARA_ERR_CONFIG;
+    return MARA_OK;
+}
+
+static void make_grid(const MaraGpuConfig* c, GridDesc* G)
+{
+    const int n[3] = {c->ni, c->nj, c->nk};
+    std::memset(G, 0, sizeof(*G));
+    double dx[3];
+    for (int a = 0; a < 3; ++a) {
+        G->n[a] = n[a];
+        G->g[a] = c->ng[a];
+        G->N[a] = n[a] + 2 * c->ng[a];
+        dx[a] = (c->upper[a] - c->lower[a]) / n[a];
+    }
+    G->nq = c->law == MARA_LAW_HYDRO ? 5 : 8;
+    G->sP = (long long) G->N[0] * G->N[1] * G->N[2];
+    G->sU = (long long) n[0] * n[1] * n[2];
+    G->sF = (long long) (G->N[0] + 1) * (G->N[1] + 1) * (G->N[2] + 1);
+    G->dA[0] = dx[1] * dx[2];
+    G->dA[1] = dx[2] * dx[0];
+    G->dA[2] = dx[0] * dx[1];
+    G->dV = dx[0] * dx[1] * dx[2];
+    G->lmin = dx[0];
+    if (dx[1] < G->lmin) G->lmin = dx[1];
+    if (dx[2] < G->lmin) G->lmin = dx[2];
+    // CartesianMeshGeometry::faceNormal -> UnitVector xhat (0,0), yhat (0,pi/2),
+    // zhat (1,0); UnitVector::getCartesianComponents (UnitVector.cpp:32-39).
+    // Computed on the host with the same libm calls, so yhat keeps its
+    // cos(pi/2) = 6.1e-17 x-component.
+    const double mu[3] = {0.0, 0.0, 1.0}, phi[3] = {0.0, M_PI / 2, 0.0};
+    for (int a = 0; a < 3; ++a) {
+        const double st = std::sqrt(1 - mu[a] * mu[a]);
+        G->nrm[a][0] = st * std::cos(phi[a]);
+        G->nrm[a][1] = st * std::sin(phi[a]);
+        G->nrm[a][2] = mu[a];
+    }
+    G->bc = c->bc;
+    G->ct = (c->law != MARA_LAW_HYDRO) && !c->disable_ct;
+}
+
+// The stages of one MethodOfLinesTVD::advance on the plain path; dt is read
+// from st->dt on the device.
+static void enqueue_plain_step(MaraGpuHandle* h)
+{
+    static const double b1[1] = {1.0};
+    static const double b2[2] = {1.0, 0.5};
+    static const double b3[3] = {1.0, 1. / 4, 2. / 3};
+    const MaraGpuConfig& c = h->cfg;
+    const double* b = c.rk_order == 1 ? b1 : c.rk_order == 2 ? b2 : b3;
+    for (int rk = 0; rk < c.rk_order; ++rk) {
+        for (int a = 0; a < 3; ++a) {
+            if (h->G.n[a] <= 1) continue;
+            TimedPair tp;
+            timed_begin(h, 0, tp);
+            plain_flux(c.law, c.recon, c.riemann, a, h->G, h->pp, h->P[h->cur], h->F[a], h->st, h->stream);
+            timed_end(h, tp);
+            h->launches++;
+        }
+        TimedPair tp;
+        timed_begin(h, 1, tp);
+        plain_update(c.law, h->G, h->pp, h->P[h->cur], h->P[1 - h->cur], h->U0, h->U, h->F[0], h->F[1], h->F[2],
+                     b[rk], rk, &h->st->dt, h->st, h->stream);
+        timed_end(h, tp);
+        h->launches++;
+        h->cur = 1 - h->cur;
+    }
+}
+
+static void enqueue_step(MaraGpuHandle* h)
+{
+    if (h->mixed) {
+        mixed_set_timing(h->mixed, h->timing);
+        mixed_enqueue_step(h->mixed, &h->st->dt, h->st, h->stream, nullptr);
+        h->launches += mixed_launches_per_step(h->mixed);
+    } else {
+        enqueue_plain_step(h);
+    }
+}
+
+static void enqueue_courant(MaraGpuHandle* h)
+{
+    launch_courant_init(h->st, h->stream);
+    TimedPair tp;
+    timed_begin(h, 2, tp);
+    if (h->mixed) mixed_enqueue_courant(h->mixed, h->st, h->stream);
+    else plain_courant(h->cfg.law, h->G, h->pp, h->P[h->cur], h->st, h->stream);
+    timed_end(h, tp);
+    h->launches += 2;
+}
+
+static int read_status(MaraGpuHandle* h)
+{
+    CK(cudaMemcpyAsync(h->st_host, h->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    const DevStatus& s = *h->st_host;
+    int status = s.code;
+    if (status == 0 && s.failures > 0) status = MARA_ERR_INVERSION_FAILURE;
+    h->last_status = status;
+    return status;
+}
+
+static int clear_status(MaraGpuHandle* h)
+{
+    DevStatus z;
+    std::memset(&z, 0, sizeof(z));
+    z.first_zone = ~0ull;
+    *h->st_host = z;
+    CK(cudaMemcpyAsync(h->st, h->st_host, sizeof(DevStatus), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MARA_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int mara_gpu_create(const MaraGpuConfig* config, MaraGpuHandle** out)
+{
+    if (!config || !out) return MARA_ERR_ARGUMENT;
+    *out = nullptr;
+    int v = validate(config);
+    if (v) return v;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MARA_ERR_NO_DEVICE;
+    if (config->device < 0 || config->device >= ndev) return MARA_ERR_NO_DEVICE;
+    CK(cudaSetDevice(config->device));
+
+    MaraGpuHandle* h = new (std::nothrow) MaraGpuHandle();
+    if (!h) return MARA_ERR_ARGUMENT;
+    h->cfg = *config;
+    make_grid(config, &h->G);
+    h->pp.gamma = config->gamma;
+    h->pp.plm_theta = config->plm_theta;
+    h->pp.shenzha_A = config->shenzha_A;
+    h->pp.pressure_floor = config->pressure_floor;
+    h->pp.weno_is = config->weno_is;
+    int rc = MARA_OK;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return MARA_ERR_CUDA; }
+    if (cudaMallocHost((void**) &h->st_host, sizeof(DevStatus)) != cudaSuccess) rc = MARA_ERR_CUDA;
+    const GridDesc& G = h->G;
+    const size_t pbytes = sizeof(double) * (size_t) G.sP * G.nq;
+    if (!rc) rc = alloc(h, (void**) &h->st, sizeof(DevStatus));
+    if (!rc) rc = alloc(h, (void**) &h->stage_aos, pbytes);
+    if (!rc && config->precision == MARA_PRECISION_FP64) {
+        const size_t ubytes = sizeof(double) * (size_t) G.sU * G.nq;
+        const size_t fbytes = sizeof(double) * (size_t) G.sF * G.nq;
+        rc = alloc(h, (void**) &h->P[0], pbytes);
+        if (!rc) rc = alloc(h, (void**) &h->P[1], pbytes);
+        if (!rc) rc = alloc(h, (void**) &h->U0, ubytes);
+        if (!rc) rc = alloc(h, (void**) &h->U, ubytes);
+        for (int a = 0; a < 3 && !rc; ++a)
+            if (G.n[a] > 1) rc = alloc(h, (void**) &h->F[a], fbytes);
+    } else if (!rc) {
+        rc = mixed_create(config, G, &h->mixed, h->stream, &h->bytes);
+    }
+    if (!rc) rc = clear_status(h);
+    if (rc) { mara_gpu_destroy(h); return rc; }
+    *out = h;
+    return MARA_OK;
+}
+
+int mara_gpu_destroy(MaraGpuHandle* h)
+{
+    if (!h) return MARA_OK;
+    cudaSetDevice(h->cfg.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& tp : h->timed) { cudaEventDestroy(tp.a); cudaEventDestroy(tp.b); }
+    for (int g = 0; g < 2; ++g) if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
+    cudaFree(h->P[0]);
+    cudaFree(h->P[1]);
+    cudaFree(h->U0);
+    cudaFree(h->U);
+    for (int a = 0; a < 3; ++a) cudaFree(h->F[a]);
+    cudaFree(h->stage_aos);
+    cudaFree(h->st);
+    if (h->mixed) mixed_destroy(h->mixed);
+    if (h->st_host) cudaFreeHost(h->st_host);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MARA_OK;
+}
+
+int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
+{
+    if (!h || !P_aos) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
+    CK(cudaMemcpyAsync(h->stage_aos, P_aos, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (h->mixed) mixed_load_aos(h->mixed, h->stage_aos, h->stream);
+    else launch_aos_to_soa(h->stage_aos, h->P[h->cur], h->G, h->stream);
+    h->launches++;
+    return cuda_status(cudaGetLastError());
+}
+
+int mara_gpu_download(MaraGpuHandle* h, double* P_aos)
+{
+    if (!h || !P_aos) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
+    if (h->mixed) mixed_store_aos(h->mixed, h->stage_aos, h->stream);
+    else launch_soa_to_aos(h->P[h->cur], h->stage_aos, h->G, h->stream);
+    h->launches++;
+    CK(cudaMemcpyAsync(P_aos, h->stage_aos, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MARA_OK;
+}
+
+int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
+{
+    (void) t0;
+    if (!h) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    launch_set_dt(h->st, dt, h->stream);
+    h->launches++;
+    enqueue_step(h);
+    h->steps++;
+    return cuda_status(cudaGetLastError());
+}
+
+int mara_gpu_advance_host(MaraGpuHandle* h, double* P_aos, double t0, double dt)
+{
+    int rc = mara_gpu_upload(h, P_aos);
+    if (!rc) rc = mara_gpu_advance(h, t0, dt);
+    if (!rc) rc = mara_gpu_download(h, P_aos);
+    if (!rc) rc = read_status(h);
+    return rc;
+}
+
+int mara_gpu_courant(MaraGpuHandle* h, double* dt)
+{
+    if (!h || !dt) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    enqueue_courant(h);
+    const int rc = read_status(h);
+    *dt = __builtin_bit_cast(double, h->st_host->dt_bits);
+    return rc;
+}
+
+static int build_run_graph(MaraGpuHandle* h, int which, double cfl, double t_final)
+{
+    cudaGraph_t g;
+    const int timing = h->timing;
+    h->timing = 0;
+    const int64_t launches = h->launches;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_courant(h);
+    launch_dt_from_courant(h->st, cfl, t_final, h->stream);
+    enqueue_step(h);
+    launch_advance_time(h->st, h->stream);
+    CK(cudaStreamEndCapture(h->stream, &g));
+    h->timing = timing;
+    h->launches = launches;
+    if (h->graph[which]) cudaGraphExecDestroy(h->graph[which]);
+    const cudaError_t e = cudaGraphInstantiate(&h->graph[which], g, 0);
+    cudaGraphDestroy(g);
+    return cuda_status(e);
+}
+
+static int launches_per_run_step(MaraGpuHandle* h)
+{
+    int n = 2 /* courant init + courant */ + 2 /* dt, time */;
+    if (h->mixed) return n + mixed_launches_per_step(h->mixed);
+    for (int a = 0; a < 3; ++a) if (h->G.n[a] > 1) n += h->cfg.rk_order;
+    return n + h->cfg.rk_order;
+}
+
+int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, double* t, int* steps_done)
+{
+    if (!h || !t) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    k_run_begin<<<1, 1, 0, h->stream>>>(h->st, *t);
+    h->launches++;
+    const bool use_graph = !h->timing;
+    if (use_graph && (h->graph_cfl != cfl || h->graph_tfinal != t_final)) {
+        for (int g = 0; g < 2; ++g) if (h->graph[g]) { cudaGraphExecDestroy(h->graph[g]); h->graph[g] = nullptr; }
+        h->graph_cfl = cfl;
+        h->graph_tfinal = t_final;
+    }
+    for (int n = 0; n < max_steps; ++n) {
+        if (use_graph) {
+            // the P ping-pong parity decides which of two captured graphs applies
+            const int which = h->mixed ? mixed_parity(h->mixed) : h->cur;
+            if (!h->graph[which]) {
+                const int cur0 = h->cur;
+                const int par0 = h->mixed ? mixed_parity(h->mixed) : 0;
+                int rc = build_run_graph(h, which, cfl, t_final);
+                if (rc) return rc;
+                h->cur = cur0;
+                if (h->mixed) mixed_set_parity(h->mixed, par0);
+            }
+            CK(cudaGraphLaunch(h->graph[which], h->stream));
+            // advance the host-side parity exactly as the captured step did
+            if (h->mixed) mixed_advance_parity(h->mixed);
+            else h->cur = (h->cur + h->cfg.rk_order) & 1;
+            h->launches += launches_per_run_step(h);
+        } else {
+            enqueue_courant(h);
+            launch_dt_from_courant(h->st, cfl, t_final, h->stream);
+            enqueue_step(h);
+            launch_advance_time(h->st, h->stream);
+            h->launches += 2;
+        }
+        h->steps++;
+    }
+    const int rc = read_status(h);
+    *t = h->st_host->t;
+    if (steps_done) *steps_done = (int) h->st_host->steps;
+    return rc;
+}
+
+int mara_gpu_synchronize(MaraGpuHandle* h)
+{
+    if (!h) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    return read_status(h);
+}
+
+int mara_gpu_stats(MaraGpuHandle* h, MaraGpuStats* s)
+{
+    if (!h || !s) return MARA_ERR_ARGUMENT;
+    const int rc = read_status(h);
+    const DevStatus& d = *h->st_host;
+    std::memset(s, 0, sizeof(*s));
+    s->status = rc;
+    s->failures = d.failures;
+    if (d.failures > 0 && d.first_zone != ~0ull) {
+        const unsigned long long z = d.first_zone;
+        const int n0 = h->G.n[0], n1 = h->G.n[1];
+        s->first_zone[0] = (int) (z % n0);
+        s->first_zone[1] = (int) ((z / n0) % n1);
+        s->first_zone[2] = (int) (z / ((unsigned long long) n0 * n1));
+        s->first_code = d.first_code;
+    }
+    s->steps = h->steps;
+    s->kernel_launches = h->launches;
+    s->last_dt = d.dt;
+    return MARA_OK;
+}
+
+void* mara_gpu_stream(MaraGpuHandle* h) { return h ? (void*) h->stream : nullptr; }
+
+int mara_gpu_set_kernel_timing(MaraGpuHandle* h, int enable)
+{
+    if (!h) return MARA_ERR_ARGUMENT;
+    h->timing = enable ? 1 : 0;
+    return MARA_OK;
+}
+
+int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches[3])
+{
+    if (!h) return MARA_ERR_ARGUMENT;
+    CK(cudaStreamSynchronize(h->stream));
+    for (auto& tp : h->timed) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, tp.a, tp.b);
+        h->ms_total[tp.cls] += ms;
+        h->timed_launches[tp.cls] += 1;
+        cudaEventDestroy(tp.a);
+        cudaEventDestroy(tp.b);
+    }
+    h->timed.clear();
+    if (h->mixed) mixed_kernel_times(h->mixed, h->ms_total, h->timed_launches);
+    for (int c = 0; c < 3; ++c) {
+        if (ms_total) ms_total[c] = h->ms_total[c];
+        if (launches) launches[c] = h->timed_launches[c];
+        h->ms_total[c] = 0;
+        h->timed_launches[c] = 0;
+    }
+    return MARA_OK;
+}
+
+int64_t mara_gpu_device_bytes(const MaraGpuHandle* h) { return h ? h->bytes : 0; }
+
+const char* mara_gpu_status_string(int s)
+{
+    switch (s) {
+        case MARA_OK: return "success";
+        case MARA_C2P_CONS_CONTAINS_NAN: return "input conserved state contained nan's";
+        case MARA_C2P_CONS_NEGATIVE_DENSITY: return "input conserved state has negative density";
+        case MARA_C2P_CONS_NEGATIVE_ENERGY: return "input conserved state has negative energy";
+        case MARA_C2P_PRIM_CONTAINS_NAN: return "derived primitive state contains nan's";
+        case MARA_C2P_PRIM_NEGATIVE_PRESSURE: return "derived primitive state has negative pressure";
+        case MARA_C2P_PRIM_NEGATIVE_RESTMASS: return "derived primitive state contains negative density";
+        case MARA_C2P_PRIM_SUPERLUMINAL: return "derived primitive state contains superluminal velocity";
+        case MARA_C2P_MAXITER: return "rootfinder hit maximum iterations";
+        case MARA_ERR_INVERSION_FAILURE: return "primitive variable inversion failed in one or more zones";
+        case MARA_ERR_SUPERLUMINAL: return "got superluminal velocity";
+        case MARA_ERR_BAD_EIGENVALUES: return "got bad eigenvalues";
+        case MARA_ERR_GUARD_TOO_SMALL: return "Boundary region of mesh data is smaller than the scheme's stencil";
+        case MARA_ERR_CONFIG: return "invalid configuration";
+        case MARA_ERR_CUDA: return "a CUDA runtime call failed";
+        case MARA_ERR_NO_DEVICE: return "no CUDA device";
+        case MARA_ERR_ARGUMENT: return "invalid argument";
+        case MARA_ERR_TOO_LARGE: return "size exceeds the supported maximum";
+        default: return "unknown status";
+    }
+}
+
+} // extern "C"

@@ -1,0 +1,27 @@
+// mixed.h -- the mixed-precision path's interface to the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mara_gpu.h"
+#include "internal.h"
+
+namespace mara {
+
+struct MixedState;
+
+int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cudaStream_t s, int64_t* bytes);
+void mixed_destroy(MixedState* m);
+void mixed_load_aos(MixedState* m, const double* aos, cudaStream_t s);
+void mixed_store_aos(MixedState* m, double* aos, cudaStream_t s);
+void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t* timed);
+void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);
+int mixed_launches_per_step(const MixedState* m);
+int mixed_parity(const MixedState* m);
+void mixed_set_parity(MixedState* m, int p);
+void mixed_advance_parity(MixedState* m);
+void mixed_set_timing(MixedState* m, int on);
+void mixed_kernel_times(MixedState* m, double ms[3], int64_t launches[3]);
+
+} // namespace mara

@@ -1,0 +1,126 @@
+"""Python host API over the C ABI: one ``Solver`` per resident grid.
+
+``Solver`` holds a ``MaraGpuHandle``: the device state of one MeshData plus
+the scheme that advances it.  Host arrays are the reference's MeshData::P
+layout (numpy float64, shape ``Scheme.full_shape``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .scheme import Scheme
+
+
+class Solver:
+    def __init__(self, scheme: Scheme, precision: str = "fp64", device: int = 0):
+        self.scheme = scheme
+        self.precision = precision
+        self.lib = N.load()
+        self._cfg = N.config_from_scheme(scheme, precision, device)
+        h = C.c_void_p()
+        N.check(self.lib.mara_gpu_create(C.byref(self._cfg), C.byref(h)), "mara_gpu_create")
+        self.h = h
+        self.t = 0.0
+
+    # -- life cycle ---------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mara_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state ----------------------------------------------------------------------
+    def upload(self, P: np.ndarray) -> None:
+        P = self._as_state(P)
+        N.check(self.lib.mara_gpu_upload(self.h, P.ctypes.data), "mara_gpu_upload")
+
+    def upload_ptr(self, ptr: int) -> None:
+        N.check(self.lib.mara_gpu_upload(self.h, C.c_void_p(ptr)), "mara_gpu_upload")
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.scheme.full_shape, dtype=np.float64)
+        N.check(self.lib.mara_gpu_download(self.h, out.ctypes.data), "mara_gpu_download")
+        return out
+
+    def download_ptr(self, ptr: int) -> None:
+        N.check(self.lib.mara_gpu_download(self.h, C.c_void_p(ptr)), "mara_gpu_download")
+
+    def _as_state(self, P):
+        if P.shape != self.scheme.full_shape or P.dtype != np.float64 or not P.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"state must be C-contiguous float64 {self.scheme.full_shape}")
+        return P
+
+    # -- stepping -------------------------------------------------------------------
+    def advance(self, dt: float, t0: float = 0.0) -> None:
+        N.check(self.lib.mara_gpu_advance(self.h, t0, dt), "mara_gpu_advance")
+
+    def advance_host(self, P: np.ndarray, dt: float, t0: float = 0.0) -> None:
+        """SolutionScheme::advance on a host MeshData::P array, in place."""
+        P = self._as_state(P)
+        N.check(self.lib.mara_gpu_advance_host(self.h, P.ctypes.data, t0, dt), "mara_gpu_advance_host")
+
+    def advance_host_ptr(self, ptr: int, dt: float, t0: float = 0.0) -> int:
+        return self.lib.mara_gpu_advance_host(self.h, C.c_void_p(ptr), t0, dt)
+
+    def courant(self) -> float:
+        dt = C.c_double()
+        N.check(self.lib.mara_gpu_courant(self.h, C.byref(dt)), "mara_gpu_courant")
+        return dt.value
+
+    def run(self, steps: int, cfl: float | None = None, t_final: float | None = None) -> int:
+        """Device-resident driver loop; returns steps taken and updates self.t."""
+        s = self.scheme
+        cfl = s.cfl if cfl is None else cfl
+        tf = -1.0 if t_final is None else t_final
+        t = C.c_double(self.t)
+        n = C.c_int(0)
+        N.check(self.lib.mara_gpu_run(self.h, steps, cfl, tf, C.byref(t), C.byref(n)), "mara_gpu_run")
+        self.t = t.value
+        return n.value
+
+    def run_async(self, steps: int, cfl: float, t_final: float | None = None) -> int:
+        """Enqueue steps without reading the status back is not offered by the
+        ABI; mara_gpu_run synchronises once at its end."""
+        return self.run(steps, cfl, t_final)
+
+    def synchronize(self) -> None:
+        N.check(self.lib.mara_gpu_synchronize(self.h), "mara_gpu_synchronize")
+
+    def stats(self) -> N.MaraGpuStats:
+        st = N.MaraGpuStats()
+        self.lib.mara_gpu_stats(self.h, C.byref(st))
+        return st
+
+    def status(self) -> int:
+        return self.lib.mara_gpu_synchronize(self.h)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.mara_gpu_stream(self.h)
+
+    def device_bytes(self) -> int:
+        return self.lib.mara_gpu_device_bytes(self.h)
+
+    def set_kernel_timing(self, on: bool) -> None:
+        self.lib.mara_gpu_set_kernel_timing(self.h, int(on))
+
+    def kernel_times(self):
+        ms = (C.c_double * 3)()
+        n = (C.c_int64 * 3)()
+        self.lib.mara_gpu_kernel_times(self.h, ms, n)
+        return list(ms), list(n)

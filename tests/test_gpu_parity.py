@@ -1,0 +1,125 @@
+"""Plain FP64 GPU path against the oracle (which is pinned bit-for-bit to the
+reference's own build): the same seeded inputs, the same dt sequence, then the
+relative L1 difference of every conserved field must be <= 1e-12, and for
+laws without transcendental eigenvalues the primitive arrays match bit for
+bit.  Calls go through the C ABI (mara2_gb300/_native.py)."""
+import numpy as np
+import pytest
+
+from helpers import oracle_config, rel_l1
+from mara2_gb300 import workloads as W
+from mara2_gb300.scheme import Scheme
+from mara2_gb300.solver import Solver
+
+TOL = 1e-12  # relative L1 per conserved field, stated by the plain-path contract
+
+
+def _cases():
+    out = []
+    s, P = W.sod(256)
+    out.append(("sod256-plm-hlle-rk2", s, P, 30))
+    s, P = W.kelvin_helmholtz(48)
+    out.append(("kh48-plm-hllc-rk2", s, P, 8))
+    out.append(("kh48-pcm-hlle-rk1-reflect", s.with_(recon="pcm", riemann="hlle", rk_order=1, bc="reflecting", guard=2), P, 8))
+    out.append(("kh48-plm-hlle-rk3-outflow", s.with_(riemann="hlle", rk_order=3, bc="outflow"), P, 6))
+    s, P = W.mhd_turbulence(12, rk_order=3)
+    out.append(("mhd12cube-plm-hlle-rk3-ct", s, P, 4))
+    out.append(("mhd12cube-noct", s.with_(disable_ct=True, rk_order=2), P, 3))
+    s, P = W.rmhd_blast(24)
+    out.append(("rmhd24-weno5-hlle-rk3", s, P, 4))
+    return out
+
+
+CASES = _cases()
+
+
+def _oracle_dts(port, s, P, steps):
+    c = oracle_config(s)
+    Q = P.copy()
+    status, t, dts = port.run(c, Q, steps, s.cfl, s.t_final)
+    assert status == 0
+    return Q, dts
+
+
+def _conserved(port, s, P):
+    st, U = port.generate_conserved(oracle_config(s), np.ascontiguousarray(P))
+    assert st == 0
+    return U[s.interior()]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,s,P,steps", CASES, ids=[c[0] for c in CASES])
+def test_advance_matches_oracle(gpu_lib, port, name, s, P, steps):
+    ref, dts = _oracle_dts(port, s, P, steps)
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        for dt in dts:
+            g.advance(dt)
+        g.synchronize()
+        out = g.download()
+    err = rel_l1(_conserved(port, s, out), _conserved(port, s, ref))
+    assert np.all(err <= TOL), (name, err)
+    if s.law != "rmhd":
+        assert np.array_equal(out[s.interior()].view(np.uint64), ref[s.interior()].view(np.uint64)), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,s,P,steps", CASES[:3], ids=[c[0] for c in CASES[:3]])
+def test_courant_matches_oracle(gpu_lib, port, name, s, P, steps):
+    st, dt_ref = port.courant(oracle_config(s), np.ascontiguousarray(P))
+    assert st == 0
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        assert g.courant() == dt_ref
+
+
+@pytest.mark.gpu
+def test_device_driver_loop_matches_oracle(gpu_lib, port):
+    """mara_gpu_run (dt = min(cfl*courant, t_final - t) on the device) against
+    the oracle's driver loop, through the end time."""
+    s, P = W.sod(128)
+    s = s.with_(t_final=0.02)
+    ref, dts = _oracle_dts(port, s, P, 10_000)
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        n = g.run(len(dts) + 5, s.cfl, s.t_final)
+        out = g.download()
+    assert n == len(dts)
+    assert abs(g.t - sum(dts)) <= 1e-15
+    assert np.array_equal(out.view(np.uint64)[s.interior()], ref.view(np.uint64)[s.interior()])
+
+
+@pytest.mark.gpu
+def test_advance_host_dropin(gpu_lib, port):
+    """The drop-in form: host MeshData::P in, advanced P out."""
+    s, P = W.kelvin_helmholtz(32)
+    ref, dts = _oracle_dts(port, s, P, 3)
+    Q = P.copy()
+    with Solver(s, "fp64") as g:
+        for dt in dts:
+            g.advance_host(Q, dt)
+    assert np.array_equal(Q[s.interior()].view(np.uint64), ref[s.interior()].view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_uniform_state_is_bit_identical(gpu_lib):
+    """TestSuite.cpp:1476-1488: a uniform state is unchanged by advance(dt=1)."""
+    s = Scheme(law="hydro", recon="plm", bc="periodic", rk_order=2, shape=(16, 16, 1))
+    P = np.zeros(s.full_shape)
+    P[..., 0] = 1.0
+    P[..., 4] = 1.0
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        g.advance(1.0)
+        out = g.download()
+    assert np.array_equal(out, P)
+
+
+@pytest.mark.gpu
+def test_guard_too_small_is_rejected(gpu_lib):
+    """TestSuite.cpp:1491-1511: guards thinner than the stencil throw."""
+    from mara2_gb300 import _native as N
+    s = Scheme(law="hydro", recon="plm", shape=(32, 1, 1), guard=1)
+    with pytest.raises(N.MaraError) as e:
+        Solver(s, "fp64")
+    assert e.value.code == N.MARA_ERR_GUARD_TOO_SMALL
