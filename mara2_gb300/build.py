@@ -26,8 +26,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I" + os.path.join(HERE, "..", "include")] + ARCH
 UNITS = {
     "plain_fp64.cu": ["--fmad=false"],
-    "mixed.cu": ["--fmad=true"],
-    "batch.cu": ["--fmad=true"],
+    "mixed.cu": ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "batch.cu": ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "mara_gpu.cu": ["--fmad=false"],
     "no_alloc.cu": ["--fmad=false"],
 }

@@ -371,7 +371,7 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
     CK(cudaSetDevice(h->cfg.device));
     const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
     CK(cudaMemcpyAsync(h->stage_aos, P_aos, bytes, cudaMemcpyHostToDevice, h->stream));
-    if (h->mixed) mixed_load_aos(h->mixed, h->stage_aos, h->stream);
+    if (h->mixed) mixed_load_aos(h->mixed, h->stage_aos, h->st, h->stream);
     else launch_aos_to_soa(h->stage_aos, h->P[h->cur], h->G, h->stream);
     h->launches++;
     return cuda_status(cudaGetLastError());

@@ -1,18 +1,693 @@
-// mixed.cu -- placeholder until the mixed-precision kernels land.
+// mixed.cu -- the mixed-precision path of one grid.
+//
+// State: conserved densities as FP32 pairs (hi + lo), SoA over the interior,
+// in a rotation of three buffers (see hydro_tile.cuh).  Two kernel families:
+//
+//  * fused tiles (hydro_tile.cuh) for Newtonian hydro on 1-D / 2-D grids:
+//    one kernel per RK stage, primitives and fluxes in shared memory only;
+//  * the general form for every law / reconstruction / dimension: one FP32
+//    face-flux kernel per axis (FP32 fluxes in HBM), then an update kernel
+//    doing FP32 flux CT, divergence, the FP32-pair RK combine and the
+//    primitive recovery (FP32 for hydro and MHD, FP64 Newton for RMHD), and
+//    writing FP32 primitives with their guard images for the next sweep.
+#include <cfloat>
+#include <cstring>
+#include <vector>
+
+#include "hydro_tile.cuh"
 #include "mixed.h"
+#include "physics_fp32.cuh"
 
 namespace mara {
-struct MixedState { int parity; };
-int mixed_create(const MaraGpuConfig*, const GridDesc&, MixedState** out, cudaStream_t, int64_t*) { *out = nullptr; return MARA_ERR_CONFIG; }
-void mixed_destroy(MixedState*) {}
-void mixed_load_aos(MixedState*, const double*, cudaStream_t) {}
-void mixed_store_aos(MixedState*, double*, cudaStream_t) {}
-void mixed_enqueue_step(MixedState*, const double*, DevStatus*, cudaStream_t, int64_t*) {}
-void mixed_enqueue_courant(MixedState*, DevStatus*, cudaStream_t) {}
-int mixed_launches_per_step(const MixedState*) { return 0; }
-int mixed_parity(const MixedState* m) { return m->parity; }
-void mixed_set_parity(MixedState* m, int p) { m->parity = p; }
-void mixed_advance_parity(MixedState*) {}
-void mixed_set_timing(MixedState*, int) {}
-void mixed_kernel_times(MixedState*, double*, int64_t*) {}
+
+// ---------------------------------------------------------------------------
+// general form
+struct GridF {
+    int n[3], g[3], N[3];
+    long long sP, sU, sF;
+    float nrm[3][3];
+    float idx[3];      // 1/dx per axis
+    float lmin;
+    int bc, ct;
+    float gamma, plm_theta, shenzha_A, pressure_floor;
+    int weno_is;
+    double gamma_d, pfloor_d;
+};
+
+template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 1 : RECON == RECON_PLM ? 2 : 3; };
+
+template <int LAW, int RECON, int RIEMANN>
+__global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P, float* __restrict__ F, GridF G,
+                                                     int axis, int lo0, int lo1, int lo2, int nb0,
+                                                     const int* __restrict__ done, DevStatus* st)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    constexpr int S = SOf<RECON>::S;
+    if (*done || st->code) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb0) return;
+    const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
+    const long long stride = axis == 0 ? 1 : axis == 1 ? (long long) G.N[0] : (long long) G.N[0] * G.N[1];
+    const long long base = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    const float n[3] = {G.nrm[axis][0], G.nrm[axis][1], G.nrm[axis][2]};
+    float PL[NQ], PR[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        float v[2 * S];
+#pragma unroll
+        for (int c = 0; c < 2 * S; ++c) v[c] = P[q * G.sP + base + (c - S) * stride];
+        if constexpr (RECON == RECON_PCM) { PL[q] = v[0]; PR[q] = v[1]; }
+        else if constexpr (RECON == RECON_PLM) {
+            PL[q] = v[1] + 0.5f * minmod_f(G.plm_theta, v[0], v[1], v[2]);
+            PR[q] = v[2] - 0.5f * minmod_f(G.plm_theta, v[1], v[2], v[3]);
+        } else {
+            PL[q] = weno5_f<true>(&v[2], G.weno_is, G.shenzha_A);
+            PR[q] = weno5_f<false>(&v[3], G.weno_is, G.shenzha_A);
+        }
+    }
+    StateF<NQ> L, R;
+    int e = law_prim_f<LAW>(G.gamma, PL, n, L);
+    if (e == ST_OK) e = law_prim_f<LAW>(G.gamma, PR, n, R);
+    if (e != ST_OK) { atomicCAS(&st->code, 0, e); return; }
+    float Fh[NQ];
+    if constexpr (RIEMANN == RIEMANN_HLLC) hllc_f<NQ>(L, R, n, Fh);
+    else hlle_f<NQ>(L, R, Fh);
+    const long long f = ((long long) k * (G.N[1] + 1) + j) * (G.N[0] + 1) + i;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) F[q * G.sF + f] = Fh[q];
 }
+
+struct FluxViewF {
+    const float* F[3];
+    long long sF;
+    int M0, M1;
+    __device__ __forceinline__ float at(int a, int q, int i, int j, int k) const
+    {
+        return F[a][q * sF + ((long long) k * M1 + j) * M0 + i];
+    }
+};
+
+// flux CT of CellCenteredFieldCT::correctGodunovFluxes on one face (FP32)
+template <int NQ>
+__device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G, int a, int q, int i, int j, int k)
+{
+    if (NQ == 8 && G.ct && q >= 5) {
+        const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
+        const int B0 = 5, B1 = 6, B2 = 7;
+        if (a == 0) {
+            if (q == B0) return 0.f;
+            if (q == B1 && fy)
+                return 0.125f * (2.f * V.at(0, B1, i, j, k) + V.at(0, B1, i, j + 1, k) + V.at(0, B1, i, j - 1, k)
+                                 - V.at(1, B0, i, j + 1, k) - V.at(1, B0, i - 1, j + 1, k)
+                                 - V.at(1, B0, i, j, k) - V.at(1, B0, i - 1, j, k));
+            if (q == B2 && fz)
+                return 0.125f * (2.f * V.at(0, B2, i, j, k) + V.at(0, B2, i, j, k + 1) + V.at(0, B2, i, j, k - 1)
+                                 - V.at(2, B0, i, j, k + 1) - V.at(2, B0, i - 1, j, k + 1)
+                                 - V.at(2, B0, i, j, k) - V.at(2, B0, i - 1, j, k));
+        } else if (a == 1) {
+            if (q == B1) return 0.f;
+            if (q == B2 && fz)
+                return 0.125f * (2.f * V.at(1, B2, i, j, k) + V.at(1, B2, i, j, k + 1) + V.at(1, B2, i, j, k - 1)
+                                 - V.at(2, B1, i, j, k + 1) - V.at(2, B1, i, j - 1, k + 1)
+                                 - V.at(2, B1, i, j, k) - V.at(2, B1, i, j - 1, k));
+            if (q == B0 && fx)
+                return 0.125f * (2.f * V.at(1, B0, i, j, k) + V.at(1, B0, i + 1, j, k) + V.at(1, B0, i - 1, j, k)
+                                 - V.at(0, B1, i + 1, j, k) - V.at(0, B1, i + 1, j - 1, k)
+                                 - V.at(0, B1, i, j, k) - V.at(0, B1, i, j - 1, k));
+        } else {
+            if (q == B2) return 0.f;
+            if (q == B0 && fx)
+                return 0.125f * (2.f * V.at(2, B0, i, j, k) + V.at(2, B0, i + 1, j, k) + V.at(2, B0, i - 1, j, k)
+                                 - V.at(0, B2, i + 1, j, k) - V.at(0, B2, i + 1, j, k - 1)
+                                 - V.at(0, B2, i, j, k) - V.at(0, B2, i, j, k - 1));
+            if (q == B1 && fy)
+                return 0.125f * (2.f * V.at(2, B1, i, j, k) + V.at(2, B1, i, j + 1, k) + V.at(2, B1, i, j - 1, k)
+                                 - V.at(1, B2, i, j + 1, k) - V.at(1, B2, i, j + 1, k - 1)
+                                 - V.at(1, B2, i, j, k) - V.at(1, B2, i, j, k - 1));
+        }
+    }
+    return V.at(a, q, i, j, k);
+}
+
+__device__ __forceinline__ int guard_images_m(int ii, int n, int g, int bc, int* out, int* flip)
+{
+    int c = 0;
+    out[c] = ii + g; flip[c] = 0; ++c;
+    if (g == 0) return c;
+    if (bc == BC_PERIODIC) {
+        if (ii < g) { out[c] = ii + g + n; flip[c] = 0; ++c; }
+        if (ii >= n - g) { out[c] = ii + g - n; flip[c] = 0; ++c; }
+    } else if (bc == BC_OUTFLOW) {
+        if (ii == 0) for (int m = 0; m < g; ++m) { out[c] = m; flip[c] = 0; ++c; }
+        if (ii == n - 1) for (int m = 0; m < g; ++m) { out[c] = n + g + m; flip[c] = 0; ++c; }
+    } else {
+        if (ii < g) { out[c] = g - 1 - ii; flip[c] = 1; ++c; }
+        if (ii >= n - g) { out[c] = 2 * n + g - 1 - ii; flip[c] = 1; ++c; }
+    }
+    return c;
+}
+
+// primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
+// ConsToPrimRMHD for RMHD (the Newton iteration keeps FP64)
+template <int LAW>
+__device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    if constexpr (LAW == LAW_HYDRO) {
+        float U[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) U[q] = Un[q].hi + Un[q].lo;
+        hydro_cons_f(G.gamma, U, P);
+        return ST_OK;
+    } else if constexpr (LAW == LAW_MHD) {
+        float U[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) U[q] = Un[q].hi + Un[q].lo;
+        const int e = mhd_cons_f(G.gamma, G.pressure_floor, U, P);
+        *code = e;
+        return e;
+    } else {
+        double U[NQ], Pd[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) U[q] = df_to_double(Un[q]);
+        PhysParams pp;
+        pp.gamma = G.gamma_d;
+        pp.pressure_floor = G.pfloor_d;
+        pp.plm_theta = 0.0;
+        pp.shenzha_A = 0.0;
+        pp.weno_is = 0;
+        // the Newton solve, without the eigenvalue evaluation of the closing
+        // fromPrimitive call (its FP32 counterpart runs in the flux kernels)
+        C2pRmhd s;
+        s.gamf = (pp.gamma - 1.0) / pp.gamma;
+        s.pfloor = pp.pressure_floor;
+        s.D = U[0];
+        s.Tau = U[4];
+        s.S2 = U[1] * U[1] + U[2] * U[2] + U[3] * U[3];
+        s.B2 = U[5] * U[5] + U[6] * U[6] + U[7] * U[7];
+        s.BS = U[5] * U[1] + U[6] * U[2] + U[7] * U[3];
+        s.BS2 = s.BS * s.BS;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s.Cons[q] = U[q];
+        s.Z_start = sqrt(s.S2 + s.D * s.D);
+        s.W_start = s.Z_start / s.D;
+        int err = rm_anton2dzw(s, Pd);
+        if (err != ST_OK) err = rm_noble1dw(s, Pd);
+        if (err != ST_OK) { *code = err; return ST_INVERSION_FAILURE; }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) P[q] = (float) Pd[q];
+        return ST_OK;
+    }
+}
+
+template <int LAW>
+__global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, float* const* Uh, float* const* Ul,
+                                                       int s_buf, int src, int dst, FluxViewF V, GridF G,
+                                                       const double* __restrict__ dtp, float b, float omb,
+                                                       const int* __restrict__ done, DevStatus* st)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    if (*done || st->code) return;
+    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ii >= G.n[0]) return;
+    const int jj = blockIdx.y, kk = blockIdx.z;
+    const int i = ii + G.g[0], j = jj + G.g[1], k = kk + G.g[2];
+    const long long uc = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
+    const float dt = (float) *dtp;
+    const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
+    df Un[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        float L = 0.f;
+        if (fx) L -= (face_flux_f<NQ>(V, G, 0, q, i + 1, j, k) - face_flux_f<NQ>(V, G, 0, q, i, j, k)) * G.idx[0];
+        if (fy) L -= (face_flux_f<NQ>(V, G, 1, q, i, j + 1, k) - face_flux_f<NQ>(V, G, 1, q, i, j, k)) * G.idx[1];
+        if (fz) L -= (face_flux_f<NQ>(V, G, 2, q, i, j, k + 1) - face_flux_f<NQ>(V, G, 2, q, i, j, k)) * G.idx[2];
+        const df U0 = {Uh[s_buf][q * G.sU + uc], Ul[s_buf][q * G.sU + uc]};
+        const df Up = {Uh[src][q * G.sU + uc], Ul[src][q * G.sU + uc]};
+        Un[q] = rk_combine(U0, Up, dt * L, b, omb);
+        Uh[dst][q * G.sU + uc] = Un[q].hi;
+        Ul[dst][q * G.sU + uc] = Un[q].lo;
+    }
+    float Pn[NQ];
+    int code = ST_OK;
+    const long long pc = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    const int e = recover_mixed<LAW>(G, Un, Pn, &code);
+    if (e == ST_INVERSION_FAILURE) {
+        atomicAdd(&st->failures, 1);
+        const unsigned long long z = (unsigned long long) uc;
+        const unsigned long long prev = atomicMin(&st->first_zone, z);
+        if (z < prev) atomicExch(&st->first_code, code);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) Pn[q] = Pf[q * G.sP + pc];
+    }
+    int ix[4], iy[4], iz[4], sx[4], sy[4], sz[4];
+    const int cx = guard_images_m(ii, G.n[0], G.g[0], G.bc, ix, sx);
+    const int cy = guard_images_m(jj, G.n[1], G.g[1], G.bc, iy, sy);
+    const int cz = guard_images_m(kk, G.n[2], G.g[2], G.bc, iz, sz);
+    for (int c = 0; c < cz; ++c)
+        for (int bb = 0; bb < cy; ++bb)
+            for (int a = 0; a < cx; ++a) {
+                const long long o = ((long long) iz[c] * G.N[1] + iy[bb]) * G.N[0] + ix[a];
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    float v = Pn[q];
+                    if ((q == 1 && sx[a]) || (q == 2 && sy[bb]) || (q == 3 && sz[c])) v = -v;
+                    Pf[q * G.sP + o] = v;
+                }
+            }
+}
+
+template <int LAW>
+__global__ void __launch_bounds__(256) courant_f_kernel(const float* __restrict__ Pf, GridF G,
+                                                        unsigned long long* __restrict__ dst, DevStatus* st)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+    float zdt = 3.0e38f;
+    if (ii < G.n[0]) {
+        const long long pc = ((long long) (blockIdx.z + G.g[2]) * G.N[1] + (blockIdx.y + G.g[1])) * G.N[0] + (ii + G.g[0]);
+        float P[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) P[q] = Pf[q * G.sP + pc];
+        float lmax = 0.f;
+        for (int a = 0; a < 3; ++a) {
+            StateF<NQ> S;
+            const int e = law_prim_f<LAW>(G.gamma, P, G.nrm[a], S);
+            if (e != ST_OK) { atomicCAS(&st->code, 0, e); break; }
+            lmax = fmaxf(lmax, fmaxf(fabsf(S.amax), fabsf(S.amin)));
+        }
+        zdt = G.lmin / lmax;
+    }
+    block_min_to(dst, zdt);
+}
+
+// AoS FP64 MeshData::P -> FP32-pair conserved state (FP64 fromPrimitive)
+// and FP32 primitives with guards
+template <int LAW>
+__global__ void load_kernel(const double* __restrict__ aos, float* Uh, float* Ul, float* Pf, GridF G, PhysParams pp,
+                            DevStatus* st)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= G.sP) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    double P[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) P[q] = aos[c * NQ + q];
+    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    if (Pf)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) Pf[q * G.sP + s] = (float) P[q];
+    const int ii = i - G.g[0], jj = j - G.g[1], kk = k - G.g[2];
+    if (ii < 0 || jj < 0 || kk < 0 || ii >= G.n[0] || jj >= G.n[1] || kk >= G.n[2]) return;
+    double U[NQ];
+    const int e = law_p2u<LAW>(pp, P, U);
+    if (e != ST_OK) atomicCAS(&st->code, 0, e);
+    const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const df d = df_from_double(U[q]);
+        Uh[q * G.sU + u] = d.hi;
+        Ul[q * G.sU + u] = d.lo;
+    }
+}
+
+// FP32-pair state -> AoS FP64 primitives with guards (FP64 fromConserved of
+// each zone's boundary image)
+template <int LAW>
+__global__ void store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos, GridF G, PhysParams pp)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= G.sP) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    int f[3] = {0, 0, 0};
+    const int ii = G.n[0] > 1 ? bc_image(i - G.g[0], G.n[0], G.bc, f[0]) : 0;
+    const int jj = G.n[1] > 1 ? bc_image(j - G.g[1], G.n[1], G.bc, f[1]) : 0;
+    const int kk = G.n[2] > 1 ? bc_image(k - G.g[2], G.n[2], G.bc, f[2]) : 0;
+    const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
+    double U[NQ], P[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) U[q] = (double) Uh[q * G.sU + u] + (double) Ul[q * G.sU + u];
+    int code = 0;
+    law_cons<LAW>(pp, U, P, &code);
+    if (f[0]) P[1] = -P[1];
+    if (f[1]) P[2] = -P[2];
+    if (f[2]) P[3] = -P[3];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) aos[c * NQ + q] = P[q];
+}
+
+__global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long long) __double_as_longlong(DBL_MAX); }
+__global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
+__global__ void k_rot_flip(int* rot) { *rot ^= 1; }
+
+// ---------------------------------------------------------------------------
+struct MixedState {
+    MaraGpuConfig cfg;
+    GridDesc G;
+    GridF GF;
+    PhysParams pp;
+    bool fused = false;
+    float* Uh[3] = {nullptr, nullptr, nullptr};
+    float* Ul[3] = {nullptr, nullptr, nullptr};
+    float** dUh = nullptr;  // device copies of the pointer tables
+    float** dUl = nullptr;
+    float* Pf = nullptr;
+    float* F[3] = {nullptr, nullptr, nullptr};
+    HGrid* dgrid = nullptr;
+    TileRef* dtiles = nullptr;
+    int ntiles = 0;
+    int* drot = nullptr;     // state buffer index (device)
+    int rot = 0;             // host mirror for the general form's parity
+    unsigned long long* dcfl = nullptr;
+    int tx = 32, ty = 16;
+    int ctas = 0;
+    int timing = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    double ms = 0;
+    int64_t nlaunch = 0;
+};
+
+static int dev_alloc(void** p, size_t bytes, cudaStream_t s, int64_t* total)
+{
+    if (cudaMalloc(p, bytes) != cudaSuccess) return MARA_ERR_CUDA;
+    cudaMemsetAsync(*p, 0, bytes, s);
+    *total += (int64_t) bytes;
+    return MARA_OK;
+}
+
+int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cudaStream_t s, int64_t* bytes)
+{
+    MixedState* m = new MixedState();
+    m->cfg = *c;
+    m->G = G;
+    GridF& F = m->GF;
+    for (int a = 0; a < 3; ++a) {
+        F.n[a] = G.n[a]; F.g[a] = G.g[a]; F.N[a] = G.N[a];
+        for (int b = 0; b < 3; ++b) F.nrm[a][b] = (float) G.nrm[a][b];
+        const double dx = (c->upper[a] - c->lower[a]) / G.n[a];
+        F.idx[a] = (float) (1.0 / dx);
+    }
+    F.sP = G.sP; F.sU = G.sU; F.sF = G.sF;
+    F.lmin = (float) G.lmin;
+    F.bc = G.bc; F.ct = G.ct;
+    F.gamma = (float) c->gamma; F.plm_theta = (float) c->plm_theta; F.shenzha_A = (float) c->shenzha_A;
+    F.pressure_floor = (float) c->pressure_floor; F.weno_is = c->weno_is;
+    F.gamma_d = c->gamma; F.pfloor_d = c->pressure_floor;
+    m->pp.gamma = c->gamma; m->pp.plm_theta = c->plm_theta; m->pp.shenzha_A = c->shenzha_A;
+    m->pp.pressure_floor = c->pressure_floor; m->pp.weno_is = c->weno_is;
+
+    m->fused = c->law == MARA_LAW_HYDRO && G.n[2] == 1 && c->recon != MARA_RECON_WENO5 && G.n[0] > 1;
+    const int nq = G.nq;
+    int rc = MARA_OK;
+    for (int b = 0; b < 3 && !rc; ++b) {
+        rc = dev_alloc((void**) &m->Uh[b], sizeof(float) * G.sU * nq, s, bytes);
+        if (!rc) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
+    }
+    if (!rc) rc = dev_alloc((void**) &m->dUh, sizeof(float*) * 3, s, bytes);
+    if (!rc) rc = dev_alloc((void**) &m->dUl, sizeof(float*) * 3, s, bytes);
+    if (!rc) rc = dev_alloc((void**) &m->drot, sizeof(int), s, bytes);
+    if (!rc) rc = dev_alloc((void**) &m->dcfl, sizeof(unsigned long long), s, bytes);
+    if (!rc) {
+        cudaMemcpyAsync(m->dUh, m->Uh, sizeof(float*) * 3, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(m->dUl, m->Ul, sizeof(float*) * 3, cudaMemcpyHostToDevice, s);
+    }
+    if (!rc && !m->fused) {
+        rc = dev_alloc((void**) &m->Pf, sizeof(float) * G.sP * nq, s, bytes);
+        for (int a = 0; a < 3 && !rc; ++a)
+            if (G.n[a] > 1) rc = dev_alloc((void**) &m->F[a], sizeof(float) * G.sF * nq, s, bytes);
+    }
+    if (!rc && m->fused) {
+        HGrid h;
+        std::memset(&h, 0, sizeof(h));
+        for (int b = 0; b < 3; ++b) { h.Uh[b] = m->Uh[b]; h.Ul[b] = m->Ul[b]; }
+        h.sU = G.sU;
+        h.n0 = G.n[0];
+        h.n1 = G.n[1];
+        h.bc = G.bc;
+        h.gamma = (float) c->gamma;
+        h.plm_theta = (float) c->plm_theta;
+        h.idx = F.idx[0];
+        h.idy = F.idx[1];
+        h.lmin = F.lmin;
+        m->tx = G.n[1] > 1 ? 32 : 256;
+        m->ty = G.n[1] > 1 ? 16 : 1;
+        std::vector<TileRef> tiles;
+        for (int y = 0; y < G.n[1]; y += m->ty)
+            for (int x = 0; x < G.n[0]; x += m->tx) tiles.push_back({0, x, y, 0});
+        m->ntiles = (int) tiles.size();
+        rc = dev_alloc((void**) &m->dgrid, sizeof(HGrid), s, bytes);
+        if (!rc) rc = dev_alloc((void**) &m->dtiles, sizeof(TileRef) * tiles.size(), s, bytes);
+        if (!rc) {
+            cudaMemcpyAsync(m->dgrid, &h, sizeof(HGrid), cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(m->dtiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice, s);
+            cudaStreamSynchronize(s);
+        }
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        m->ctas = m->ntiles;
+    }
+    if (rc) { mixed_destroy(m); return rc; }
+    *out = m;
+    return MARA_OK;
+}
+
+void mixed_destroy(MixedState* m)
+{
+    if (!m) return;
+    for (auto& e : m->ev) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+    for (int b = 0; b < 3; ++b) { cudaFree(m->Uh[b]); cudaFree(m->Ul[b]); }
+    cudaFree(m->dUh); cudaFree(m->dUl); cudaFree(m->drot); cudaFree(m->dcfl);
+    cudaFree(m->Pf);
+    for (int a = 0; a < 3; ++a) cudaFree(m->F[a]);
+    cudaFree(m->dgrid);
+    cudaFree(m->dtiles);
+    delete m;
+}
+
+template <typename Fn>
+static void timed(MixedState* m, cudaStream_t s, Fn fn)
+{
+    if (!m->timing) { fn(); return; }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    fn();
+    cudaEventRecord(b, s);
+    m->ev.push_back({a, b});
+}
+
+static int host_rot(const MixedState* m) { return m->rot; }
+
+// Courant step straight from the FP32-pair state (fused hydro form)
+__global__ void __launch_bounds__(256) courant_u_kernel(const HGrid* __restrict__ grid, const int* __restrict__ rot,
+                                                        unsigned long long* __restrict__ dst)
+{
+    const HGrid& g = *grid;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    float zdt = 3.0e38f;
+    if (x < g.n0) {
+        const long long o = (long long) y * g.n0 + x;
+        float U[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) U[q] = g.Uh[*rot][q * g.sU + o];
+        zdt = hydro_zone_dt(g, U);
+    }
+    block_min_to(dst, zdt);
+}
+
+static void courant_general(MixedState* m, DevStatus* st, cudaStream_t s)
+{
+    dim3 grid((m->G.n[0] + 255) / 256, m->G.n[1], m->G.n[2]);
+    switch (m->cfg.law) {
+        case MARA_LAW_HYDRO: courant_f_kernel<LAW_HYDRO><<<grid, 256, 0, s>>>(m->Pf, m->GF, m->dcfl, st); break;
+        case MARA_LAW_MHD: courant_f_kernel<LAW_MHD><<<grid, 256, 0, s>>>(m->Pf, m->GF, m->dcfl, st); break;
+        default: courant_f_kernel<LAW_RMHD><<<grid, 256, 0, s>>>(m->Pf, m->GF, m->dcfl, st); break;
+    }
+}
+
+void mixed_load_aos(MixedState* m, const double* aos, DevStatus* st, cudaStream_t s)
+{
+    const long long n = m->G.sP;
+    const int r = host_rot(m);
+    cudaMemcpyAsync(m->drot, &m->rot, sizeof(int), cudaMemcpyHostToDevice, s);
+    const unsigned nb = (unsigned) ((n + 255) / 256);
+    switch (m->cfg.law) {
+        case MARA_LAW_HYDRO: load_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
+        case MARA_LAW_MHD: load_kernel<LAW_MHD><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
+        default: load_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
+    }
+    // Courant step of the loaded state, published by mixed_enqueue_courant
+    k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
+    if (m->fused) {
+        dim3 grid((m->G.n[0] + 255) / 256, m->G.n[1], 1);
+        courant_u_kernel<<<grid, 256, 0, s>>>(m->dgrid, m->drot, m->dcfl);
+    } else {
+        courant_general(m, st, s);
+    }
+}
+
+void mixed_store_aos(MixedState* m, double* aos, cudaStream_t s)
+{
+    const long long n = m->G.sP;
+    const unsigned nb = (unsigned) ((n + 255) / 256);
+    const int r = host_rot(m);
+    switch (m->cfg.law) {
+        case MARA_LAW_HYDRO: store_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
+        case MARA_LAW_MHD: store_kernel<LAW_MHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
+        default: store_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
+    }
+}
+
+// ---- general form ------------------------------------------------------------
+template <int LAW, int RECON, int RIEMANN>
+static void flux_f_launch(MixedState* m, int axis, const int* done, DevStatus* st, cudaStream_t s)
+{
+    const GridF& G = m->GF;
+    int lo[3], nb[3];
+    for (int a = 0; a < 3; ++a) {
+        if (a == axis) { lo[a] = G.g[a]; nb[a] = G.n[a] + 1; }
+        else if (G.n[a] > 1) { const int e = G.ct ? 1 : 0; lo[a] = G.g[a] - e; nb[a] = G.n[a] + 2 * e; }
+        else { lo[a] = 0; nb[a] = 1; }
+    }
+    dim3 grid((nb[0] + 127) / 128, nb[1], nb[2]);
+    flux_f_kernel<LAW, RECON, RIEMANN><<<grid, 128, 0, s>>>(m->Pf, m->F[axis], G, axis, lo[0], lo[1], lo[2], nb[0], done, st);
+}
+
+template <int LAW, int RECON>
+static void flux_f_r(MixedState* m, int axis, const int* done, DevStatus* st, cudaStream_t s)
+{
+    if (m->cfg.riemann == MARA_RIEMANN_HLLC) flux_f_launch<LAW, RECON, RIEMANN_HLLC>(m, axis, done, st, s);
+    else flux_f_launch<LAW, RECON, RIEMANN_HLLE>(m, axis, done, st, s);
+}
+
+template <int LAW>
+static void flux_f(MixedState* m, int axis, const int* done, DevStatus* st, cudaStream_t s)
+{
+    switch (m->cfg.recon) {
+        case MARA_RECON_PCM: flux_f_r<LAW, RECON_PCM>(m, axis, done, st, s); break;
+        case MARA_RECON_PLM: flux_f_r<LAW, RECON_PLM>(m, axis, done, st, s); break;
+        default: flux_f_r<LAW, RECON_WENO5>(m, axis, done, st, s); break;
+    }
+}
+
+static const float B_TAB[3][3] = {{1.f, 0.f, 0.f}, {1.f, 0.5f, 0.f}, {1.f, 0.25f, 2.f / 3.f}};
+
+static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s)
+{
+    const int order = m->cfg.rk_order;
+    const int* done = &st->done;
+    FluxViewF V;
+    for (int a = 0; a < 3; ++a) V.F[a] = m->F[a];
+    V.sF = m->G.sF;
+    V.M0 = m->G.N[0] + 1;
+    V.M1 = m->G.N[1] + 1;
+    const int sb = 0, tb = 1;
+    for (int rk = 0; rk < order; ++rk) {
+        for (int a = 0; a < 3; ++a) {
+            if (m->G.n[a] <= 1) continue;
+            timed(m, s, [&] {
+                switch (m->cfg.law) {
+                    case MARA_LAW_HYDRO: flux_f<LAW_HYDRO>(m, a, done, st, s); break;
+                    case MARA_LAW_MHD: flux_f<LAW_MHD>(m, a, done, st, s); break;
+                    default: flux_f<LAW_RMHD>(m, a, done, st, s); break;
+                }
+            });
+        }
+        const float b = B_TAB[order - 1][rk];
+        const int src = rk == 0 ? sb : tb;
+        const int dst = rk == order - 1 ? sb : tb;
+        dim3 grid((m->G.n[0] + 127) / 128, m->G.n[1], m->G.n[2]);
+        timed(m, s, [&] {
+            switch (m->cfg.law) {
+                case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
+                case MARA_LAW_MHD: update_f_kernel<LAW_MHD><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
+                default: update_f_kernel<LAW_RMHD><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
+            }
+        });
+    }
+    // Courant step of the new state for the next step
+    k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
+    courant_general(m, st, s);
+}
+
+// ---- fused hydro tiles ------------------------------------------------------
+template <int DIM, int RECON, int RIEMANN>
+static void tile_launch(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int stage, float b, int last)
+{
+    constexpr int TX = DIM == 2 ? 32 : 256, TY = DIM == 2 ? 16 : 1, NT = 256;
+    hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT><<<m->ctas, NT, 0, s>>>(
+        m->dgrid, m->dtiles, m->ntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+}
+
+template <int DIM>
+static void tile_dispatch(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int stage, float b, int last)
+{
+    const bool hllc = m->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (m->cfg.recon == MARA_RECON_PCM) {
+        if (hllc) tile_launch<DIM, RECON_PCM, RIEMANN_HLLC>(m, dt, st, s, stage, b, last);
+        else tile_launch<DIM, RECON_PCM, RIEMANN_HLLE>(m, dt, st, s, stage, b, last);
+    } else {
+        if (hllc) tile_launch<DIM, RECON_PLM, RIEMANN_HLLC>(m, dt, st, s, stage, b, last);
+        else tile_launch<DIM, RECON_PLM, RIEMANN_HLLE>(m, dt, st, s, stage, b, last);
+    }
+}
+
+static void fused_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s)
+{
+    const int order = m->cfg.rk_order;
+    for (int rk = 0; rk < order; ++rk) {
+        const int last = rk == order - 1;
+        if (last) k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
+        const float b = B_TAB[order - 1][rk];
+        timed(m, s, [&] {
+            if (m->G.n[1] > 1) tile_dispatch<2>(m, dt, st, s, rk, b, last);
+            else tile_dispatch<1>(m, dt, st, s, rk, b, last);
+        });
+    }
+    if (order == 1) k_rot_flip<<<1, 1, 0, s>>>(m->drot);
+}
+
+void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t*)
+{
+    if (m->fused) fused_step(m, dt, st, s);
+    else general_step(m, dt, st, s);
+    if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1;
+}
+
+int mixed_launches_per_step(const MixedState* m)
+{
+    if (m->fused) return m->cfg.rk_order + 1 + (m->cfg.rk_order == 1 ? 1 : 0);
+    int axes = 0;
+    for (int a = 0; a < 3; ++a) axes += m->G.n[a] > 1;
+    return m->cfg.rk_order * (axes + 1) + 2;
+}
+
+void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s) { k_cfl_publish<<<1, 1, 0, s>>>(m->dcfl, st); }
+int mixed_parity(const MixedState* m) { return m->rot & 1; }
+void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
+void mixed_advance_parity(MixedState* m) { if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1; }
+void mixed_set_timing(MixedState* m, int on) { m->timing = on; }
+
+void mixed_kernel_times(MixedState* m, double ms[3], int64_t launches[3])
+{
+    for (auto& e : m->ev) {
+        float t = 0.f;
+        cudaEventSynchronize(e.second);
+        cudaEventElapsedTime(&t, e.first, e.second);
+        ms[0] += t;
+        launches[0] += 1;
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    m->ev.clear();
+}
+
+} // namespace mara

@@ -13,7 +13,7 @@ struct MixedState;
 
 int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cudaStream_t s, int64_t* bytes);
 void mixed_destroy(MixedState* m);
-void mixed_load_aos(MixedState* m, const double* aos, cudaStream_t s);
+void mixed_load_aos(MixedState* m, const double* aos, DevStatus* st, cudaStream_t s);
 void mixed_store_aos(MixedState* m, double* aos, cudaStream_t s);
 void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t* timed);
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);

@@ -97,7 +97,7 @@ int mo_stencil_size(const mo_config* c)
     }
 }
 
-static int make_geom(const mo_config* c, mgeom* g)
+static int make_geom_chk(const mo_config* c, mgeom* g, int check_stencil)
 {
     const int n[3] = {c->ni, c->nj, c->nk};
     const int s = mo_stencil_size(c);
@@ -108,7 +108,7 @@ static int make_geom(const mo_config* c, mgeom* g)
         if (n[a] < 1 || c->ng[a] < 0) return MO_ERR_CONFIG;
         if (n[a] == 1 && c->ng[a] != 0) return MO_ERR_CONFIG;
         /* SchemeHelpers::makeFootprint (SolutionSchemes.cpp:17-49) */
-        if (n[a] > 1 && c->ng[a] < s) return MO_ERR_GUARD_TOO_SMALL;
+        if (check_stencil && n[a] > 1 && c->ng[a] < s) return MO_ERR_GUARD_TOO_SMALL;
         g->N[a] = n[a] + 2 * c->ng[a];
         g->dx[a] = (c->upper[a] - c->lower[a]) / n[a];
     }
@@ -123,6 +123,11 @@ static int make_geom(const mo_config* c, mgeom* g)
     mo_face_normals(g->nrm);
     return MO_OK;
 }
+
+/* geometry for whole-array passes; the stencil footprint is checked only
+ * where a flux sweep runs (SchemeHelpers::makeFootprint is called by
+ * MethodOfLinesTVD::advance alone) */
+static int make_geom(const mo_config* c, mgeom* g) { return make_geom_chk(c, g, 0); }
 
 static inline long cidx(const mgeom* g, int i, int j, int k)
 {
@@ -1037,7 +1042,7 @@ static int use_ct(const mo_config* c)
 int mo_godunov(const mo_config* c, const double* P, double* F)
 {
     mgeom g;
-    int err = make_geom(c, &g);
+    int err = make_geom_chk(c, &g, 1);
     if (err) return err;
     if ((err = godunov_sweeps(c, &g, P, F))) return err;
     if (use_ct(c)) mo_ct_correct(F, g.N[0] + 1, g.N[1] + 1, g.N[2] + 1, g.nq, 5);
@@ -1202,7 +1207,7 @@ int mo_advance(const mo_config* c, double* P, double t0, double dt, mo_failure* 
     static const double b3[3] = {1.0, 1. / 4, 2. / 3};
     const double* b;
     mgeom g;
-    int err = make_geom(c, &g);
+    int err = make_geom_chk(c, &g, 1);
     long ncell, nelem, fsize;
     double *U0, *U, *F, *L;
     (void) t0;

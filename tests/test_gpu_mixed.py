@@ -1,0 +1,83 @@
+"""Mixed-precision path against the FP64 oracle.
+
+FP32 reconstruction / Riemann / flux arithmetic with an FP32-pair conserved
+accumulator must stay within the stated tolerance of the FP64 reference on
+the same inputs and the same dt sequence: relative L1 density error <= 1e-5
+(the precision contract), checked here over short runs where it is met with
+a wide margin, for every law and both kernel families."""
+import numpy as np
+import pytest
+
+from helpers import oracle_config, rel_l1
+from mara2_gb300 import workloads as W
+from mara2_gb300.solver import Solver
+
+TOL_RHO = 1e-5  # relative L1 of the density against the FP64 oracle
+
+
+def _cases():
+    out = []
+    s, P = W.sod(512)
+    out.append(("sod512-fused", s, P, 60))
+    s, P = W.kelvin_helmholtz(96)
+    out.append(("kh96-fused-hllc", s, P, 20))
+    out.append(("kh96-fused-hlle-rk3", s.with_(riemann="hlle", rk_order=3), P, 10))
+    # guards must agree with the boundary condition, as the reference's drivers
+    # ensure by calling applyBoundaryCondition after generating initial data
+    sr = s.with_(recon="pcm", rk_order=1, bc="reflecting", guard=2)
+    out.append(("kh96-fused-pcm-rk1-reflect", sr, W.apply_bc_numpy(sr, P.copy()), 10))
+    so = s.with_(bc="outflow")
+    out.append(("kh96-fused-plm-outflow", so, W.apply_bc_numpy(so, P.copy()), 10))
+    s, P = W.mhd_turbulence(16, rk_order=3)
+    out.append(("mhd16cube-general-ct", s, P, 6))
+    s, P = W.rmhd_blast(48)
+    out.append(("rmhd48-general-weno5", s, P, 6))
+    return out
+
+
+CASES = _cases()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,s,P,steps", CASES, ids=[c[0] for c in CASES])
+def test_mixed_close_to_fp64_oracle(gpu_lib, port, name, s, P, steps):
+    c = oracle_config(s)
+    ref = P.copy()
+    status, _, dts = port.run(c, ref, steps, s.cfl, s.t_final)
+    assert status == 0
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        for dt in dts:
+            g.advance(dt)
+        g.synchronize()
+        out = g.download()
+    err = rel_l1(out[s.interior()], ref[s.interior()])
+    assert err[0] <= TOL_RHO, (name, err)
+    assert np.all(np.isfinite(out))
+
+
+@pytest.mark.gpu
+def test_mixed_driver_loop_runs_to_end_time(gpu_lib, port):
+    s, P = W.sod(256)
+    s = s.with_(t_final=0.05)
+    c = oracle_config(s)
+    ref = P.copy()
+    _, t_ref, dts = port.run(c, ref, 100_000, s.cfl, s.t_final)
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        n = g.run(len(dts) + 50, s.cfl, s.t_final)
+        out = g.download()
+    assert abs(g.t - s.t_final) < 1e-12
+    assert abs(n - len(dts)) <= 2          # FP32 Courant steps may differ slightly
+    err = rel_l1(out[s.interior()], ref[s.interior()])
+    assert err[0] < 1e-4, err
+
+
+@pytest.mark.gpu
+def test_mixed_courant_close(gpu_lib, port):
+    s, P = W.kelvin_helmholtz(64)
+    _, dt_ref = port.courant(oracle_config(s), P.copy())
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        dt = g.courant()
+    assert abs(dt - dt_ref) / dt_ref < 1e-6

@@ -1,0 +1,144 @@
+"""The oracle restatement (oracle/mara_oracle.c) against the reference's own
+hot-path sources compiled in place (oracle/_ref): bit-for-bit on whole
+advances, fluxes, Courant steps, guard fills and point operations.  Skipped
+where the reference tree is absent."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import oracle_config
+from mara2_gb300 import workloads as W
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if not O.ref_available():
+        try:
+            O.build(ref=True)
+        except Exception:
+            pytest.skip("reference tree not available")
+    if not O.ref_available():
+        pytest.skip("reference tree not available")
+    return O.Oracle("ref")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+CASES = [
+    ("sod", lambda: W.sod(96), {}, 30),
+    ("sod-pcm-rk1", lambda: W.sod(64), dict(recon="pcm", rk_order=1), 20),
+    ("sod-plm-hllc-rk3", lambda: W.sod(64), dict(riemann="hllc", rk_order=3), 20),
+    ("sod-theta2", lambda: W.sod(64), dict(plm_theta=2.0), 10),
+    ("kh", lambda: W.kelvin_helmholtz(20), {}, 6),
+    ("kh-reflect", lambda: W.kelvin_helmholtz(20), dict(bc="reflecting"), 6),
+    ("kh-outflow-hlle", lambda: W.kelvin_helmholtz(20), dict(bc="outflow", riemann="hlle"), 6),
+    ("mhd3d", lambda: W.mhd_turbulence(8), {}, 3),
+    ("mhd3d-noct", lambda: W.mhd_turbulence(8), dict(disable_ct=True), 2),
+    ("mhd3d-floor", lambda: W.mhd_turbulence(8), dict(pressure_floor=1e-3), 2),
+    ("rmhd-weno-js", lambda: W.rmhd_blast(16), dict(weno_is="js96"), 2),
+    ("rmhd-weno-borges", lambda: W.rmhd_blast(16), dict(weno_is="borges08"), 2),
+    ("rmhd-weno-shenzha", lambda: W.rmhd_blast(16), {}, 3),
+    ("rmhd-plm", lambda: W.rmhd_blast(16), dict(recon="plm"), 3),
+]
+
+
+@pytest.mark.parametrize("name,make,kw,steps", CASES, ids=[c[0] for c in CASES])
+def test_advance_bitwise(port, ref, name, make, kw, steps):
+    s, P = make()
+    s = s.with_(**kw)
+    c = oracle_config(s)
+    A, B = P.copy(), P.copy()
+    sa, _, da = port.run(c, A, steps, s.cfl, s.t_final)
+    sb, _, db = ref.run(c, B, steps, s.cfl, s.t_final)
+    assert sa == sb == 0
+    assert da == db
+    assert np.array_equal(_bits(A), _bits(B))
+
+
+@pytest.mark.parametrize("make", [lambda: W.kelvin_helmholtz(12), lambda: W.mhd_turbulence(6), lambda: W.rmhd_blast(12)])
+def test_godunov_fluxes_bitwise(port, ref, make):
+    s, P = make()
+    c = oracle_config(s)
+    sa, Fa = port.godunov(c, P.copy())
+    sb, Fb = ref.godunov(c, P.copy())
+    assert sa == sb == 0
+    assert np.array_equal(_bits(Fa), _bits(Fb))
+
+
+def test_bc_and_conserved_bitwise(port, ref):
+    for bc in ("periodic", "outflow", "reflecting"):
+        s, P = W.kelvin_helmholtz(10)
+        s = s.with_(bc=bc)
+        c = oracle_config(s)
+        rng = np.random.default_rng(5)
+        P = P + 0.01 * rng.random(P.shape)
+        A, B = P.copy(), P.copy()
+        assert port.apply_bc(c, A) == ref.apply_bc(c, B) == 0
+        assert np.array_equal(_bits(A), _bits(B))
+        sa, Ua = port.generate_conserved(c, A)
+        sb, Ub = ref.generate_conserved(c, B)
+        assert np.array_equal(_bits(Ua), _bits(Ub))
+
+
+def test_point_operations_bitwise(port, ref):
+    rng = np.random.default_rng(7)
+    c = O.make_config(law="rmhd", gamma=4.0 / 3)
+    for _ in range(200):
+        v = rng.uniform(-0.5, 0.5, 3)
+        P = [rng.uniform(0.1, 2), *v, rng.uniform(0.01, 3), *rng.uniform(-2, 2, 3)]
+        n = [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0)][rng.integers(3)]
+        a = port.from_primitive(c, P, n)
+        b = ref.from_primitive(c, P, n)
+        assert a[0] == b[0]
+        for x, y in zip(a[1:], b[1:]):
+            assert np.array_equal(_bits(x), _bits(y))
+        if a[0] == 0:
+            ra = port.from_conserved(c, a[1][:8])
+            rb = ref.from_conserved(c, b[1][:8])
+            assert ra[0] == rb[0]
+            assert np.array_equal(_bits(ra[1]), _bits(rb[1]))
+    for _ in range(200):
+        d = rng.uniform(-3, 3, 5)
+        na, ra = port.quartic(*d)
+        nb, rb = ref.quartic(*d)
+        assert na == nb and np.array_equal(_bits(ra), _bits(rb))
+
+
+def test_ct_and_monopole_bitwise(port, ref):
+    rng = np.random.default_rng(11)
+    for shape in [(9, 9, 2, 8), (7, 6, 5, 8), (8, 2, 2, 8)]:
+        F = rng.standard_normal(shape + (3,))
+        assert np.array_equal(_bits(port.ct_correct(F)), _bits(ref.ct_correct(F)))
+    B = rng.standard_normal((6, 5, 4, 3))
+    assert np.array_equal(_bits(port.monopole_cell(B, 0.5)), _bits(ref.monopole_cell(B, 0.5)))
+
+
+def test_failure_reporting_matches(port, ref):
+    """A zone that cannot be inverted: same status, count and first zone."""
+    s, P = W.mhd_turbulence(6)
+    c = oracle_config(s)
+    P = P.copy()
+    P[4, 5, 3, 4] = 1e-9       # near-vacuum pressure next to strong gradients
+    P[4, 5, 3, 1] = 3.0
+    A, B = P.copy(), P.copy()
+    sa, fa = port.advance(c, A, 0.05)
+    sb, fb = ref.advance(c, B, 0.05)
+    assert sa == sb
+    assert fa.count == fb.count
+    if fa.count:
+        assert tuple(fa.first) == tuple(fb.first)
+
+
+def test_workload_vector_potential_matches_reference(ref):
+    """workloads.vector_potential_to_cell_b restates Problems.cpp:660-667."""
+    s, _ = W.mhd_turbulence(6)
+    A = W.face_vector_potential(s, lambda x, y, z: W._fourier_vector(5, x, y, z))
+    B = W.vector_potential_to_cell_b(s, A)
+    c = oracle_config(s)
+    Bref = np.zeros(B.shape)
+    import ctypes as C
+    ref.lib.mr_vector_potential_to_cell_b(C.byref(c), np.ascontiguousarray(A).ctypes.data_as(C.POINTER(C.c_double)),
+                                          Bref.ctypes.data_as(C.POINTER(C.c_double)))
+    np.testing.assert_allclose(B, Bref, rtol=0, atol=1e-12 * np.abs(Bref).max())
