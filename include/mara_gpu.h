@@ -130,6 +130,11 @@ int mara_gpu_courant(MaraGpuHandle* h, double* dt);
  * no end time).  dt never leaves the device.  *t is read and updated. */
 int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, double* t, int* steps_done);
 
+/* The same loop without waiting: the steps are enqueued on the handle's
+ * stream and the call returns at once (t and the status are read by the next
+ * mara_gpu_run, mara_gpu_synchronize or mara_gpu_stats). */
+int mara_gpu_run_async(MaraGpuHandle* h, int max_steps, double cfl, double t_final);
+
 /* Wait for the handle's stream; returns the first error seen. */
 int mara_gpu_synchronize(MaraGpuHandle* h);
 int mara_gpu_stats(MaraGpuHandle* h, MaraGpuStats* stats);

@@ -61,6 +61,7 @@ SIGNATURES = {
     "mara_gpu_advance_host": (C.c_int, [_H, C.c_void_p, C.c_double, C.c_double]),
     "mara_gpu_courant": (C.c_int, [_H, _D]),
     "mara_gpu_run": (C.c_int, [_H, C.c_int, C.c_double, C.c_double, _D, C.POINTER(C.c_int)]),
+    "mara_gpu_run_async": (C.c_int, [_H, C.c_int, C.c_double, C.c_double]),
     "mara_gpu_synchronize": (C.c_int, [_H]),
     "mara_gpu_stats": (C.c_int, [_H, C.POINTER(MaraGpuStats)]),
     "mara_gpu_stream": (C.c_void_p, [_H]),

@@ -449,12 +449,8 @@ static int launches_per_run_step(MaraGpuHandle* h)
     return n + h->cfg.rk_order;
 }
 
-int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, double* t, int* steps_done)
+static int enqueue_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final)
 {
-    if (!h || !t) return MARA_ERR_ARGUMENT;
-    CK(cudaSetDevice(h->cfg.device));
-    k_run_begin<<<1, 1, 0, h->stream>>>(h->st, *t);
-    h->launches++;
     const bool use_graph = !h->timing;
     if (use_graph && (h->graph_cfl != cfl || h->graph_tfinal != t_final)) {
         for (int g = 0; g < 2; ++g) if (h->graph[g]) { cudaGraphExecDestroy(h->graph[g]); h->graph[g] = nullptr; }
@@ -487,10 +483,28 @@ int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, do
         }
         h->steps++;
     }
-    const int rc = read_status(h);
+    return cuda_status(cudaGetLastError());
+}
+
+int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, double* t, int* steps_done)
+{
+    if (!h || !t) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    k_run_begin<<<1, 1, 0, h->stream>>>(h->st, *t);
+    h->launches++;
+    int rc = enqueue_run(h, max_steps, cfl, t_final);
+    if (rc) return rc;
+    rc = read_status(h);
     *t = h->st_host->t;
     if (steps_done) *steps_done = (int) h->st_host->steps;
     return rc;
+}
+
+int mara_gpu_run_async(MaraGpuHandle* h, int max_steps, double cfl, double t_final)
+{
+    if (!h) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    return enqueue_run(h, max_steps, cfl, t_final);
 }
 
 int mara_gpu_synchronize(MaraGpuHandle* h)

@@ -93,10 +93,12 @@ class Solver:
         self.t = t.value
         return n.value
 
-    def run_async(self, steps: int, cfl: float, t_final: float | None = None) -> int:
-        """Enqueue steps without reading the status back is not offered by the
-        ABI; mara_gpu_run synchronises once at its end."""
-        return self.run(steps, cfl, t_final)
+    def run_async(self, steps: int, cfl: float | None = None, t_final: float | None = None) -> None:
+        """Enqueue steps of the driver loop on the handle's stream and return
+        at once (continues from the device-side time of the last run)."""
+        cfl = self.scheme.cfl if cfl is None else cfl
+        tf = -1.0 if t_final is None else t_final
+        N.check(self.lib.mara_gpu_run_async(self.h, steps, cfl, tf), "mara_gpu_run_async")
 
     def synchronize(self) -> None:
         N.check(self.lib.mara_gpu_synchronize(self.h), "mara_gpu_synchronize")
