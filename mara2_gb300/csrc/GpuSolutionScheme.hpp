@@ -1,0 +1,185 @@
+// GpuSolutionScheme.hpp -- the drop-in for Mara2: a SolutionScheme whose
+// advance() runs on the GPU through the C ABI of include/mara_gpu.h.
+//
+// Header-only C++14, meant to be compiled inside a Mara2 build (it includes
+// the reference's own interface headers).  It keeps the reference's
+// dependency-injection surface (Mara.hpp:44-51, SolutionSchemes.hpp:24-72):
+// setBoundaryCondition / setFieldOperator / setMeshOperator /
+// setIntercellFluxScheme / setRungeKuttaOrder / setDisableFieldCT, and maps
+// the injected objects onto the GPU configuration by their dynamic type.
+// Parameters the reference classes keep without getters (the gamma-law index,
+// the PLM theta, the Riemann solver inside a flux scheme, the pressure floor,
+// the mesh bounds) are given once in Options.
+//
+// Errors come back as the reference's exception types:
+//   FieldOperator::InversionFailure for failed primitive recoveries,
+//   std::runtime_error for superluminal states / bad eigenvalues,
+//   std::logic_error for configuration errors (guards smaller than the
+//   stencil, missing operators, unsupported types).
+#pragma once
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <typeinfo>
+
+#include "BoundaryConditions.hpp"
+#include "CartesianMeshGeometry.hpp"
+#include "ConservationLaws.hpp"
+#include "FieldOperator.hpp"
+#include "IntercellFluxSchemes.hpp"
+#include "Mara.hpp"
+#include "MeshData.hpp"
+#include "MeshOperator.hpp"
+#include "mara_gpu.h"
+
+struct GpuSchemeOptions
+{
+    double gammaLawIndex = 5. / 3;   // ConservationLaw::setGammaLawIndex
+    double plmTheta = 1.5;           // MethodOfLinesPlm default
+    double pressureFloor = -1.0;     // ConservationLaw::setPressureFloor
+    int riemannSolver = MARA_RIEMANN_HLLE;
+    int wenoSmoothness = MARA_WENO_SHENZHA10;
+    double shenZha10A = 50.0;
+    Coordinate lower = {{0.0, 0.0, 0.0}};  // CartesianMeshGeometry::setLowerUpper
+    Coordinate upper = {{1.0, 1.0, 1.0}};
+    int precision = MARA_PRECISION_FP64;
+    int device = 0;
+};
+
+class GpuMethodOfLinesTVD : public SolutionScheme
+{
+public:
+    using Options = GpuSchemeOptions;
+
+    GpuMethodOfLinesTVD() {}
+    explicit GpuMethodOfLinesTVD (Options options) : opts (options) {}
+    ~GpuMethodOfLinesTVD() { if (handle) mara_gpu_destroy (handle); }
+    GpuMethodOfLinesTVD (const GpuMethodOfLinesTVD&) = delete;
+    GpuMethodOfLinesTVD& operator= (const GpuMethodOfLinesTVD&) = delete;
+
+    void setRungeKuttaOrder (int order)
+    {
+        if (0 >= order || order > 3) throw std::logic_error ("Runge-Kutta order not 1, 2, or 3");
+        rungeKuttaOrder = order;
+        reset();
+    }
+    void setDisableFieldCT (bool disable) { disableFieldCT = disable; reset(); }
+    void setBoundaryCondition (std::shared_ptr<BoundaryCondition> bc) override { boundaryCondition = bc; reset(); }
+    void setFieldOperator (std::shared_ptr<FieldOperator> fo) override { fieldOperator = fo; reset(); }
+    void setMeshOperator (std::shared_ptr<MeshOperator> mo) override { meshOperator = mo; reset(); }
+    void setIntercellFluxScheme (std::shared_ptr<IntercellFluxScheme> fs) override { fluxScheme = fs; reset(); }
+
+    int getStencilSize() const override
+    {
+        if (! fluxScheme) throw std::logic_error ("No IntercellFluxScheme instance");
+        return fluxScheme->getStencilSize();
+    }
+
+    /** MethodOfLinesTVD::advance on solution.P (host, in place). */
+    void advance (MeshData& solution, double t0, double dt) const override
+    {
+        ensure (solution);
+        raise (mara_gpu_advance_host (handle, solution.P.data(), t0, dt));
+    }
+
+    /** FieldOperator::getCourantTimestep of solution.P (interior), on the GPU. */
+    double getCourantTimestep (MeshData& solution) const
+    {
+        ensure (solution);
+        raise (mara_gpu_upload (handle, solution.P.data()));
+        double dt = 0.0;
+        raise (mara_gpu_courant (handle, &dt));
+        return dt;
+    }
+
+private:
+    void reset() { if (handle) { mara_gpu_destroy (handle); handle = nullptr; } }
+
+    void ensure (MeshData& solution) const
+    {
+        if (handle) return;
+        if (! fieldOperator)     throw std::logic_error ("No FieldOperator instance");
+        if (! meshOperator)      throw std::logic_error ("No MeshOperator instance");
+        if (! boundaryCondition) throw std::logic_error ("No BoundaryCondition instance");
+        if (! fluxScheme)        throw std::logic_error ("No IntercellFluxScheme instance");
+
+        MaraGpuConfig c = {};
+        auto law = fieldOperator->getConservationLaw();
+        if      (dynamic_cast<NewtonianHydro*>  (law.get())) c.law = MARA_LAW_HYDRO;
+        else if (dynamic_cast<NewtonianMHD*>    (law.get())) c.law = MARA_LAW_MHD;
+        else if (dynamic_cast<RelativisticMHD*> (law.get())) c.law = MARA_LAW_RMHD;
+        else throw std::logic_error ("GpuMethodOfLinesTVD: unsupported ConservationLaw");
+
+        const auto* fs = fluxScheme.get();
+        if      (dynamic_cast<const MethodOfLinesPlm*> (fs)) c.recon = MARA_RECON_PLM;
+        else if (dynamic_cast<const MethodOfLines*>    (fs)) c.recon = MARA_RECON_PCM;
+        else if (fs->getStencilSize() == 3)                 c.recon = MARA_RECON_WENO5;
+        else throw std::logic_error ("GpuMethodOfLinesTVD: unsupported IntercellFluxScheme");
+
+        const auto* bc = boundaryCondition.get();
+        if      (dynamic_cast<const PeriodicBoundaryCondition*>   (bc)) c.bc = MARA_BC_PERIODIC;
+        else if (dynamic_cast<const OutflowBoundaryCondition*>    (bc)) c.bc = MARA_BC_OUTFLOW;
+        else if (dynamic_cast<const ReflectingBoundaryCondition*> (bc)) c.bc = MARA_BC_REFLECTING;
+        else throw std::logic_error ("GpuMethodOfLinesTVD: unsupported BoundaryCondition");
+
+        const auto& mg = meshOperator->getMeshGeometry();
+        if (! dynamic_cast<const CartesianMeshGeometry*> (&mg))
+            throw std::logic_error ("GpuMethodOfLinesTVD: only CartesianMeshGeometry is supported");
+        const auto cells = mg.cellsShape();
+        const auto guards = solution.getBoundaryShape();
+
+        c.riemann = opts.riemannSolver;
+        c.rk_order = rungeKuttaOrder;
+        c.disable_ct = disableFieldCT ? 1 : 0;
+        c.weno_is = opts.wenoSmoothness;
+        c.ni = cells[0]; c.nj = cells[1]; c.nk = cells[2];
+        for (int a = 0; a < 3; ++a)
+        {
+            c.ng[a] = guards[a];
+            c.lower[a] = opts.lower[a];
+            c.upper[a] = opts.upper[a];
+        }
+        c.gamma = opts.gammaLawIndex;
+        c.plm_theta = opts.plmTheta;
+        c.shenzha_A = opts.shenZha10A;
+        c.pressure_floor = opts.pressureFloor;
+        c.precision = opts.precision;
+        c.device = opts.device;
+        raise (mara_gpu_create (&c, &handle));
+    }
+
+    void raise (int status) const
+    {
+        switch (status)
+        {
+            case MARA_OK: return;
+            case MARA_ERR_INVERSION_FAILURE:
+            {
+                MaraGpuStats st;
+                mara_gpu_stats (handle, &st);
+                auto failure = FieldOperator::InversionFailure();
+                ConservationLaw::State S;
+                auto zone = ConservationLaw::StateFailure (S);
+                zone.setZoneIndex (Cow::Index {{st.first_zone[0], st.first_zone[1], st.first_zone[2], 0, 0}});
+                failure.failedStates.push_back (zone);
+                failure.updateWhatMessage();
+                throw failure;
+            }
+            case MARA_ERR_SUPERLUMINAL:
+            case MARA_ERR_BAD_EIGENVALUES:
+                throw std::runtime_error (mara_gpu_status_string (status));
+            default:
+                throw std::logic_error (std::string ("GpuMethodOfLinesTVD: ") + mara_gpu_status_string (status));
+        }
+    }
+
+    Options opts;
+    int rungeKuttaOrder = 1;
+    bool disableFieldCT = false;
+    std::shared_ptr<BoundaryCondition> boundaryCondition;
+    std::shared_ptr<FieldOperator> fieldOperator;
+    std::shared_ptr<MeshOperator> meshOperator;
+    std::shared_ptr<IntercellFluxScheme> fluxScheme;
+    mutable MaraGpuHandle* handle = nullptr;
+};

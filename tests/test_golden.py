@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import oracle_config, rel_l1
+from helpers import oracle_config, parity_error, rel_l1
 from mara2_gb300.scheme import Scheme  # noqa: F401  (eval of the stored repr)
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -49,7 +49,7 @@ def test_gpu_plain_reproduces_golden(gpu_lib, port, path):
     c = oracle_config(s)
     _, Uo = port.generate_conserved(c, np.ascontiguousarray(out))
     _, Ur = port.generate_conserved(c, np.ascontiguousarray(ref))
-    err = rel_l1(Uo[s.interior()], Ur[s.interior()])
+    err = parity_error(s, Uo[s.interior()], Ur[s.interior()])
     assert np.all(err <= 1e-12), err.tolist()
     if s.law != "rmhd":
         assert np.array_equal(out[s.interior()].view(np.uint64), ref[s.interior()].view(np.uint64))

@@ -6,7 +6,7 @@ bit.  Calls go through the C ABI (mara2_gb300/_native.py)."""
 import numpy as np
 import pytest
 
-from helpers import oracle_config, rel_l1
+from helpers import oracle_config, parity_error, rel_l1
 from mara2_gb300 import workloads as W
 from mara2_gb300.scheme import Scheme
 from mara2_gb300.solver import Solver
@@ -57,7 +57,7 @@ def test_advance_matches_oracle(gpu_lib, port, name, s, P, steps):
             g.advance(dt)
         g.synchronize()
         out = g.download()
-    err = rel_l1(_conserved(port, s, out), _conserved(port, s, ref))
+    err = parity_error(s, _conserved(port, s, out), _conserved(port, s, ref))
     print(name, "relative L1 per conserved field:", err.tolist())
     assert np.all(err <= TOL), (name, err.tolist())
     if s.law != "rmhd":
