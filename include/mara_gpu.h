@@ -151,6 +151,24 @@ int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches
 /* Device bytes the handle holds. */
 int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
 
+/* One plain-FP64 advance (the same arithmetic as mara_gpu_advance) on
+ * device buffers the caller owns, for callers that cannot allocate device
+ * memory when they step a grid: an application whose memory pool already
+ * reserves the GPU, a latency-critical loop that must not block in or fail
+ * inside an allocation, code that must avoid cudaFree's device-wide
+ * synchronisation.  P_in and P_out are device pointers to MeshData::P in the
+ * layout above (they may be the same buffer); stream may be 0.  All
+ * intermediates live in a fixed 64 MiB scratch array inside the library's
+ * device image (held on every GPU that loads the library until the process
+ * exits); grids whose intermediates exceed it return MARA_ERR_TOO_LARGE.
+ * Calls share that array, so calls whose GPU work overlaps race: order them
+ * on one stream.  The first call on a device looks the array up with the
+ * device current; make it before any stream capture.  Synchronises the
+ * stream and returns the step's status.  No counterpart in the reference:
+ * it exists for callers of this library that cannot allocate. */
+int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const double* P_in, double* P_out,
+                             double dt, void* stream);
+
 const char* mara_gpu_status_string(int status);
 
 #ifdef __cplusplus

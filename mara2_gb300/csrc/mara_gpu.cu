@@ -296,6 +296,13 @@ static int clear_status(MaraGpuHandle* h)
     return MARA_OK;
 }
 
+// configuration check and mesh description for mara_gpu_advance_noalloc
+// (no_alloc.cu), which works without a handle
+namespace mara {
+int noalloc_validate(const MaraGpuConfig* c) { return validate(c); }
+void noalloc_make_grid(const MaraGpuConfig* c, GridDesc* G) { make_grid(c, G); }
+} // namespace mara
+
 // ---------------------------------------------------------------------------
 extern "C" {
 
