@@ -1,0 +1,552 @@
+// batch.cu -- many independent hydro grids advanced together (include/
+// mara_batch.h).
+//
+// Device tables, one entry per slot: HGrid (state pointers, shape, bc,
+// gamma), the driver state (t, dt, t_final, cfl factor, done, steps, Courant
+// bits) and the buffer rotation.  Two tile lists (1-D tiles, 2-D tiles) cover
+// every resident grid; each RK stage is two persistent launches of the fused
+// stage kernel (hydro_tile.cuh), one per list, whatever mix of grids is
+// resident.  A batch step -- per-grid dt, the RK stages, the per-grid Courant
+// reduction fused into the last stage, the time update -- is captured once
+// as a CUDA graph: admitting or retiring a grid rewrites the tables and the
+// tile lists (device-resident counts), never the graph.
+//
+// Memory: each grid holds its FP32-pair state (2 rotation buffers for RK1/2,
+// 3 for RK3) allocated stream-ordered from the device's memory pool and
+// counted against the batch's HBM budget; admission fails with
+// MARA_ERR_NO_ROOM when the budget or the slot table is full.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/mara_batch.h"
+#include "hydro_tile.cuh"
+
+namespace mara {
+
+struct SlotHost {
+    bool used = false;
+    bool finished_reported = false;
+    int dims = 0, n0 = 0, n1 = 1, g0 = 0, g1 = 0;
+    int bc = 0;
+    double gamma = 5. / 3;
+    int64_t bytes = 0;
+    float* bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int64_t zones = 0;
+};
+
+__global__ void k_slot_init(HGrid* grids, int* rot, double* t, double* dt, double* tfin, double* cflp, int* done,
+                            long long* steps, int slot, HGrid g, double t_final, double cfl)
+{
+    grids[slot] = g;
+    rot[slot] = 0;
+    t[slot] = 0.0;
+    dt[slot] = 0.0;
+    tfin[slot] = t_final;
+    cflp[slot] = cfl;
+    done[slot] = 0;
+    steps[slot] = 0;
+}
+
+__global__ void k_slot_clear(int* done, int slot) { done[slot] = 1; }
+
+// per-grid dt of the drivers: dt = min(cfl * courant, t_final - t); a grid
+// whose t has reached t_final stops (MeshData left as after its last step)
+__global__ void k_batch_dt(int n, const unsigned long long* cflbits, const double* cflp, const double* t,
+                           const double* tfin, double* dt, int* done)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || done[s]) return;
+    if (!(t[s] < tfin[s])) { done[s] = 2; return; }   // 2: finished (1: empty slot)
+    const double courant = __longlong_as_double((long long) cflbits[s]);
+    double d = cflp[s] * courant;
+    const double d2 = tfin[s] - t[s];
+    dt[s] = d < d2 ? d : d2;
+}
+
+__global__ void k_batch_cfl_reset(int n, const int* done, unsigned long long* cflbits)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n && !done[s]) cflbits[s] = (unsigned long long) __double_as_longlong(DBL_MAX);
+}
+
+__global__ void k_batch_time(int n, const int* done, const double* dt, double* t, long long* steps, int* rot,
+                             int flip)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || done[s]) return;
+    t[s] += dt[s];
+    steps[s] += 1;
+    if (flip) rot[s] ^= 1;
+}
+
+__global__ void k_set_int(int* p, int v) { *p = v; }
+__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// host FP64 primitives (AoS with guards) -> FP32-pair conserved state of one
+// slot, and the grid's first Courant step
+__global__ void k_batch_load(const double* __restrict__ aos, HGrid g, int g0, int g1, int N0, int N1, double gamma,
+                             unsigned long long* cflbit)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    float zdt = 3.0e38f;
+    if (x < g.n0) {
+        const long long c = (long long) (x + g0) * N1 + (y + g1);  // AoS cell (i, j), k = 0
+        double P[5], U[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) P[q] = aos[c * 5 + q];
+        const double gm1 = gamma - 1.0;
+        const double vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
+        U[0] = P[0];
+        U[1] = P[0] * P[1];
+        U[2] = P[0] * P[2];
+        U[3] = P[0] * P[3];
+        U[4] = P[0] * 0.5 * vv + P[4] / gm1;
+        const long long o = (long long) y * g.n0 + x;
+        float Uf[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const df d = df_from_double(U[q]);
+            g.Uh[0][q * g.sU + o] = d.hi;
+            g.Ul[0][q * g.sU + o] = d.lo;
+            Uf[q] = d.hi;
+        }
+        zdt = hydro_zone_dt(g, Uf);
+    }
+    block_min_to(cflbit, zdt);
+}
+
+// FP32-pair state -> FP64 primitives (AoS with guards; guards are boundary
+// images of interior zones)
+__global__ void k_batch_store(HGrid g, int buf, int g0, int g1, int N0, int N1, double gamma, double* __restrict__ aos)
+{
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= (long long) N0 * N1) return;
+    const int j = (int) (c % N1), i = (int) (c / N1);
+    int fx = 0, fy = 0;
+    const int x = bc_image(i - g0, g.n0, g.bc, fx);
+    const int y = g.n1 > 1 ? bc_image(j - g1, g.n1, g.bc, fy) : 0;
+    const long long o = (long long) y * g.n0 + x;
+    double U[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) U[q] = (double) g.Uh[buf][q * g.sU + o] + (double) g.Ul[buf][q * g.sU + o];
+    const double gm1 = gamma - 1.0;
+    const double pp = U[1] * U[1] + U[2] * U[2] + U[3] * U[3];
+    double P[5];
+    P[0] = U[0];
+    P[4] = (U[4] - 0.5 * pp / U[0]) * gm1;
+    P[1] = U[1] / U[0];
+    P[2] = U[2] / U[0];
+    P[3] = U[3] / U[0];
+    if (fx) P[1] = -P[1];
+    if (fy) P[2] = -P[2];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) aos[c * 5 + q] = P[q];
+}
+
+} // namespace mara
+
+using namespace mara;
+
+struct MaraBatch {
+    MaraBatchConfig cfg;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+    int nslots = 0;
+    // device tables
+    HGrid* grids = nullptr;
+    int* rot = nullptr;
+    double *t = nullptr, *dt = nullptr, *tfin = nullptr, *cflp = nullptr;
+    int* done = nullptr;
+    long long* steps = nullptr;
+    unsigned long long* cflbits = nullptr;
+    TileRef* tiles[2] = {nullptr, nullptr};
+    int* ntiles = nullptr;  // [0] 1-D, [1] 2-D
+    int max_tiles[2] = {0, 0};
+    // host
+    std::vector<SlotHost> slots;
+    std::vector<int> done_host;
+    TileRef* tiles_host[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // pinned, double-buffered
+    cudaEvent_t tiles_ev[2] = {nullptr, nullptr};
+    int tiles_buf = 0;
+    bool dirty = true;
+    double* staging = nullptr;
+    int64_t staging_elems = 0;
+    int64_t bytes_in_use = 0;
+    int64_t zone_updates = 0;
+    int64_t step_count = 0;
+    int64_t launches = 0;
+    int tile1 = 256, tile2 = 2;
+    int ctas[2] = {0, 0};
+    cudaGraphExec_t graph = nullptr;
+};
+
+typedef void (*TileKernel)(const HGrid*, const TileRef*, const int*, const int*, const double*, int, const int*, int,
+                           int, float, float, int, unsigned long long*, int);
+
+template <int RECON, int RIEMANN>
+static TileKernel pick_1d(int tile)
+{
+    switch (tile) {
+        case 128: return hydro_tile_kernel<1, RECON, RIEMANN, 128, 1, 128>;
+        case 512: return hydro_tile_kernel<1, RECON, RIEMANN, 512, 1, 256>;
+        default: return hydro_tile_kernel<1, RECON, RIEMANN, 256, 1, 256>;
+    }
+}
+
+template <int RECON, int RIEMANN>
+static TileKernel pick_2d(int tile)
+{
+    switch (tile) {
+        case 1: return hydro_tile_kernel<2, RECON, RIEMANN, 32, 8, 256>;
+        case 3: return hydro_tile_kernel<2, RECON, RIEMANN, 64, 8, 256>;
+        default: return hydro_tile_kernel<2, RECON, RIEMANN, 32, 16, 256>;
+    }
+}
+
+static TileKernel kernel_for(const MaraBatch* b, int dim)
+{
+    const bool plm = b->cfg.recon == MARA_RECON_PLM, hllc = b->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (dim == 1) {
+        if (plm) return hllc ? pick_1d<RECON_PLM, RIEMANN_HLLC>(b->tile1) : pick_1d<RECON_PLM, RIEMANN_HLLE>(b->tile1);
+        return hllc ? pick_1d<RECON_PCM, RIEMANN_HLLC>(b->tile1) : pick_1d<RECON_PCM, RIEMANN_HLLE>(b->tile1);
+    }
+    if (plm) return hllc ? pick_2d<RECON_PLM, RIEMANN_HLLC>(b->tile2) : pick_2d<RECON_PLM, RIEMANN_HLLE>(b->tile2);
+    return hllc ? pick_2d<RECON_PCM, RIEMANN_HLLC>(b->tile2) : pick_2d<RECON_PCM, RIEMANN_HLLE>(b->tile2);
+}
+
+static void tile_dims(const MaraBatch* b, int dim, int* tx, int* ty, int* nt)
+{
+    if (dim == 1) { *tx = b->tile1; *ty = 1; *nt = b->tile1 == 128 ? 128 : 256; return; }
+    *nt = 256;
+    if (b->tile2 == 1) { *tx = 32; *ty = 8; }
+    else if (b->tile2 == 3) { *tx = 64; *ty = 8; }
+    else { *tx = 32; *ty = 16; }
+}
+
+static int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MARA_OK : MARA_ERR_CUDA; }
+#define BK(call) do { const cudaError_t e_ = (call); if (e_ != cudaSuccess) return MARA_ERR_CUDA; } while (0)
+
+static const float B_TABLE[3][3] = {{1.f, 0.f, 0.f}, {1.f, 0.5f, 0.f}, {1.f, 0.25f, 2.f / 3.f}};
+
+static void enqueue_batch_step(MaraBatch* b)
+{
+    const int n = b->nslots, nb = (n + 255) / 256;
+    const cudaStream_t s = b->stream;
+    k_batch_dt<<<nb, 256, 0, s>>>(n, b->cflbits, b->cflp, b->t, b->tfin, b->dt, b->done);
+    const int order = b->cfg.rk_order;
+    for (int rk = 0; rk < order; ++rk) {
+        const int last = rk == order - 1;
+        if (last) k_batch_cfl_reset<<<nb, 256, 0, s>>>(n, b->done, b->cflbits);
+        const float bb = B_TABLE[order - 1][rk];
+        for (int d = 0; d < 2; ++d) {
+            int tx, ty, nt;
+            tile_dims(b, d + 1, &tx, &ty, &nt);
+            TileKernel k = kernel_for(b, d + 1);
+            k<<<b->ctas[d], nt, 0, s>>>(b->grids, b->tiles[d], b->ntiles + d, b->rot, b->dt, 1, b->done, 1, rk, bb,
+                                        1.f - bb, last, b->cflbits, 1);
+        }
+    }
+    k_batch_time<<<nb, 256, 0, s>>>(n, b->done, b->dt, b->t, b->steps, b->rot, order == 1 ? 1 : 0);
+}
+
+static int launches_per_step(const MaraBatch* b) { return 2 + b->cfg.rk_order * 2 + 1; }
+
+static int upload_tiles(MaraBatch* b)
+{
+    // rebuild both lists from the resident grids into the free pinned buffer
+    const int which = b->tiles_buf ^ 1;
+    BK(cudaEventSynchronize(b->tiles_ev[which]));
+    int count[2] = {0, 0};
+    for (int sl = 0; sl < b->nslots; ++sl) {
+        const SlotHost& h = b->slots[sl];
+        if (!h.used || h.finished_reported) continue;
+        const int d = h.dims - 1;
+        int tx, ty, nt;
+        tile_dims(b, h.dims, &tx, &ty, &nt);
+        for (int y = 0; y < h.n1; y += ty)
+            for (int x = 0; x < h.n0; x += tx) {
+                if (count[d] >= b->max_tiles[d]) return MARA_ERR_NO_ROOM;
+                b->tiles_host[d][which][count[d]++] = {sl, x, y, 0};
+            }
+    }
+    for (int d = 0; d < 2; ++d) {
+        if (count[d]) BK(cudaMemcpyAsync(b->tiles[d], b->tiles_host[d][which], sizeof(TileRef) * count[d],
+                                         cudaMemcpyHostToDevice, b->stream));
+        k_set_int<<<1, 1, 0, b->stream>>>(b->ntiles + d, count[d]);
+    }
+    BK(cudaEventRecord(b->tiles_ev[which], b->stream));
+    b->tiles_buf = which;
+    b->dirty = false;
+    return MARA_OK;
+}
+
+extern "C" {
+
+int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
+{
+    if (!c || !out) return MARA_ERR_ARGUMENT;
+    *out = nullptr;
+    if (c->max_grids < 1 || c->hbm_budget_bytes <= 0 || c->max_zones_per_grid < 1) return MARA_ERR_CONFIG;
+    if (c->recon != MARA_RECON_PCM && c->recon != MARA_RECON_PLM) return MARA_ERR_CONFIG;
+    if (c->rk_order < 1 || c->rk_order > 3 || c->riemann < 0 || c->riemann > 1) return MARA_ERR_CONFIG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || c->device < 0 || c->device >= ndev) return MARA_ERR_NO_DEVICE;
+    BK(cudaSetDevice(c->device));
+    MaraBatch* b = new (std::nothrow) MaraBatch();
+    if (!b) return MARA_ERR_ARGUMENT;
+    b->cfg = *c;
+    b->nslots = c->max_grids;
+    b->tile1 = (c->tile_1d == 128 || c->tile_1d == 256 || c->tile_1d == 512) ? c->tile_1d : 256;
+    b->tile2 = (c->tile_2d >= 1 && c->tile_2d <= 3) ? c->tile_2d : 2;
+    b->slots.resize(b->nslots);
+    b->done_host.assign(b->nslots, 1);
+    int rc = MARA_OK;
+    auto A = [&](void** p, size_t bytes) {
+        if (rc) return;
+        if (cudaMalloc(p, bytes) != cudaSuccess) rc = MARA_ERR_CUDA;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { delete b; return MARA_ERR_CUDA; }
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int n = b->nslots;
+    A((void**) &b->grids, sizeof(HGrid) * n);
+    A((void**) &b->rot, sizeof(int) * n);
+    A((void**) &b->t, sizeof(double) * n);
+    A((void**) &b->dt, sizeof(double) * n);
+    A((void**) &b->tfin, sizeof(double) * n);
+    A((void**) &b->cflp, sizeof(double) * n);
+    A((void**) &b->done, sizeof(int) * n);
+    A((void**) &b->steps, sizeof(long long) * n);
+    A((void**) &b->cflbits, sizeof(unsigned long long) * n);
+    A((void**) &b->ntiles, sizeof(int) * 2);
+    // tile capacity: the budget bounds the zones resident at once
+    const int64_t max_zones = c->hbm_budget_bytes / 40 + 1;   // >= 2 buffers x 20 B per zone
+    b->max_tiles[0] = (int) std::min<int64_t>(max_zones / 128 + n + 16, 1 << 26);
+    b->max_tiles[1] = (int) std::min<int64_t>(max_zones / 256 + 4 * n + 16, 1 << 26);
+    for (int d = 0; d < 2; ++d) {
+        A((void**) &b->tiles[d], sizeof(TileRef) * b->max_tiles[d]);
+        for (int w = 0; w < 2 && !rc; ++w)
+            if (cudaMallocHost((void**) &b->tiles_host[d][w], sizeof(TileRef) * b->max_tiles[d]) != cudaSuccess)
+                rc = MARA_ERR_CUDA;
+    }
+    b->staging_elems = (int64_t) c->max_zones_per_grid * 5 + 1024;
+    A((void**) &b->staging, sizeof(double) * b->staging_elems);
+    for (int w = 0; w < 2 && !rc; ++w)
+        if (cudaEventCreateWithFlags(&b->tiles_ev[w], cudaEventDisableTiming) != cudaSuccess) rc = MARA_ERR_CUDA;
+    if (!rc) {
+        cudaMemsetAsync(b->done, 0, sizeof(int) * n, b->stream);
+        std::vector<int> ones(n, 1);
+        cudaMemcpy(b->done, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+        cudaMemset(b->ntiles, 0, sizeof(int) * 2);
+        cudaMemset(b->rot, 0, sizeof(int) * n);
+        for (int d = 0; d < 2; ++d) {
+            int tx, ty, nt, per = 0;
+            tile_dims(b, d + 1, &tx, &ty, &nt);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*) kernel_for(b, d + 1), nt, 0);
+            b->ctas[d] = std::max(1, per) * b->sms;
+        }
+        rc = cuda_rc(cudaDeviceSynchronize());
+    }
+    if (rc) { mara_batch_destroy(b); return rc; }
+    *out = b;
+    return MARA_OK;
+}
+
+int mara_batch_destroy(MaraBatch* b)
+{
+    if (!b) return MARA_OK;
+    cudaSetDevice(b->cfg.device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& h : b->slots)
+        for (int k = 0; k < 6; ++k)
+            if (h.bufs[k]) cudaFree(h.bufs[k]);
+    cudaFree(b->grids); cudaFree(b->rot); cudaFree(b->t); cudaFree(b->dt); cudaFree(b->tfin); cudaFree(b->cflp);
+    cudaFree(b->done); cudaFree(b->steps); cudaFree(b->cflbits); cudaFree(b->ntiles); cudaFree(b->staging);
+    for (int d = 0; d < 2; ++d) {
+        cudaFree(b->tiles[d]);
+        for (int w = 0; w < 2; ++w) if (b->tiles_host[d][w]) cudaFreeHost(b->tiles_host[d][w]);
+    }
+    for (int w = 0; w < 2; ++w) if (b->tiles_ev[w]) cudaEventDestroy(b->tiles_ev[w]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return MARA_OK;
+}
+
+int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* c, const double* P_aos, double t_final, double cfl, int* slot)
+{
+    if (!b || !c || !P_aos) return MARA_ERR_ARGUMENT;
+    if (c->law != MARA_LAW_HYDRO || c->nk != 1 || c->ni < 2) return MARA_ERR_CONFIG;
+    if (c->recon != b->cfg.recon || c->riemann != b->cfg.riemann || c->rk_order != b->cfg.rk_order) return MARA_ERR_CONFIG;
+    const int s_need = c->recon == MARA_RECON_PCM ? 1 : 2;
+    const int dims = c->nj > 1 ? 2 : 1;
+    if (c->ng[0] < s_need || (dims == 2 && c->ng[1] < s_need)) return MARA_ERR_GUARD_TOO_SMALL;
+    const int64_t zones = (int64_t) c->ni * c->nj;
+    const int N0 = c->ni + 2 * c->ng[0], N1 = c->nj + 2 * (dims == 2 ? c->ng[1] : 0);
+    if ((int64_t) N0 * N1 * 5 > b->staging_elems) return MARA_ERR_TOO_LARGE;
+    const int nbuf = b->cfg.rk_order == 3 ? 3 : 2;
+    const int64_t bytes = (int64_t) nbuf * 2 * 5 * zones * 4;
+    int sl = -1;
+    for (int k = 0; k < b->nslots; ++k)
+        if (!b->slots[k].used) { sl = k; break; }
+    if (sl < 0 || b->bytes_in_use + bytes > b->cfg.hbm_budget_bytes) return MARA_ERR_NO_ROOM;
+    BK(cudaSetDevice(b->cfg.device));
+    SlotHost& h = b->slots[sl];
+    h = SlotHost();
+    for (int k = 0; k < 2 * nbuf; ++k) {
+        if (cudaMallocAsync((void**) &h.bufs[k], sizeof(float) * 5 * zones, b->stream) != cudaSuccess) {
+            for (int j = 0; j < k; ++j) cudaFreeAsync(h.bufs[j], b->stream);
+            return MARA_ERR_NO_ROOM;
+        }
+    }
+    h.used = true;
+    h.dims = dims;
+    h.n0 = c->ni;
+    h.n1 = c->nj;
+    h.g0 = c->ng[0];
+    h.g1 = dims == 2 ? c->ng[1] : 0;
+    h.bc = c->bc;
+    h.gamma = c->gamma;
+    h.bytes = bytes;
+    h.zones = zones;
+    b->bytes_in_use += bytes;
+
+    HGrid g;
+    std::memset(&g, 0, sizeof(g));
+    for (int k = 0; k < nbuf; ++k) { g.Uh[k] = h.bufs[2 * k]; g.Ul[k] = h.bufs[2 * k + 1]; }
+    g.sU = zones;
+    g.n0 = c->ni;
+    g.n1 = c->nj;
+    g.bc = c->bc;
+    g.gamma = (float) c->gamma;
+    g.plm_theta = (float) c->plm_theta;
+    const double dx = (c->upper[0] - c->lower[0]) / c->ni, dy = (c->upper[1] - c->lower[1]) / c->nj;
+    const double dz = (c->upper[2] - c->lower[2]) / c->nk;
+    g.idx = (float) (1.0 / dx);
+    g.idy = (float) (1.0 / dy);
+    g.lmin = (float) std::min(dx, std::min(dy, dz));
+
+    BK(cudaMemcpyAsync(b->staging, P_aos, sizeof(double) * (size_t) N0 * N1 * 5, cudaMemcpyHostToDevice, b->stream));
+    k_slot_init<<<1, 1, 0, b->stream>>>(b->grids, b->rot, b->t, b->dt, b->tfin, b->cflp, b->done, b->steps, sl, g,
+                                        t_final, cfl);
+    k_set_u64<<<1, 1, 0, b->stream>>>(b->cflbits + sl, ~0ull);
+    dim3 grid((c->ni + 255) / 256, c->nj);
+    k_batch_load<<<grid, 256, 0, b->stream>>>(b->staging, g, h.g0, h.g1, N0, N1, c->gamma, b->cflbits + sl);
+    b->launches += 3;
+    b->done_host[sl] = 0;
+    b->dirty = true;
+    *slot = sl;
+    return cuda_rc(cudaGetLastError());
+}
+
+int mara_batch_step(MaraBatch* b, int steps)
+{
+    if (!b) return MARA_ERR_ARGUMENT;
+    BK(cudaSetDevice(b->cfg.device));
+    if (b->dirty) {
+        const int rc = upload_tiles(b);
+        if (rc) return rc;
+        b->launches += 2;
+    }
+    if (!b->graph) {
+        cudaGraph_t g;
+        BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_batch_step(b);
+        BK(cudaStreamEndCapture(b->stream, &g));
+        const cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        BK(e);
+    }
+    for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph, b->stream));
+    b->step_count += steps;
+    b->launches += (int64_t) steps * launches_per_step(b);
+    return MARA_OK;
+}
+
+int mara_batch_poll(MaraBatch* b, int* slots, int cap, int* n)
+{
+    if (!b || !n) return MARA_ERR_ARGUMENT;
+    BK(cudaSetDevice(b->cfg.device));
+    std::vector<int> d(b->nslots);
+    BK(cudaMemcpyAsync(d.data(), b->done, sizeof(int) * b->nslots, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    int m = 0;
+    for (int k = 0; k < b->nslots; ++k) {
+        SlotHost& h = b->slots[k];
+        if (h.used && !h.finished_reported && d[k] == 2) {
+            h.finished_reported = true;
+            b->dirty = true;  // its tiles leave the lists
+            if (m < cap && slots) slots[m] = k;
+            ++m;
+        }
+    }
+    *n = m;
+    return MARA_OK;
+}
+
+int mara_batch_retire(MaraBatch* b, int slot, double* P_aos, double* t, int64_t* steps)
+{
+    if (!b || slot < 0 || slot >= b->nslots || !b->slots[slot].used) return MARA_ERR_ARGUMENT;
+    BK(cudaSetDevice(b->cfg.device));
+    SlotHost& h = b->slots[slot];
+    const int N0 = h.n0 + 2 * h.g0, N1 = h.n1 + 2 * h.g1;
+    HGrid g;
+    std::memset(&g, 0, sizeof(g));
+    BK(cudaMemcpyAsync(&g, b->grids + slot, sizeof(HGrid), cudaMemcpyDeviceToHost, b->stream));
+    int rot = 0;
+    double tt = 0;
+    long long st = 0;
+    BK(cudaMemcpyAsync(&rot, b->rot + slot, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaMemcpyAsync(&tt, b->t + slot, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaMemcpyAsync(&st, b->steps + slot, sizeof(long long), cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    if (P_aos) {
+        const long long cells = (long long) N0 * N1;
+        k_batch_store<<<(unsigned) ((cells + 255) / 256), 256, 0, b->stream>>>(g, rot, h.g0, h.g1, N0, N1, h.gamma,
+                                                                              b->staging);
+        BK(cudaMemcpyAsync(P_aos, b->staging, sizeof(double) * cells * 5, cudaMemcpyDeviceToHost, b->stream));
+        b->launches += 1;
+    }
+    k_slot_clear<<<1, 1, 0, b->stream>>>(b->done, slot);
+    for (int k = 0; k < 6; ++k)
+        if (h.bufs[k]) cudaFreeAsync(h.bufs[k], b->stream);
+    BK(cudaStreamSynchronize(b->stream));
+    b->bytes_in_use -= h.bytes;
+    b->zone_updates += h.zones * st;
+    if (t) *t = tt;
+    if (steps) *steps = st;
+    b->done_host[slot] = 1;
+    h = SlotHost();
+    b->dirty = true;
+    return MARA_OK;
+}
+
+int mara_batch_stats(MaraBatch* b, MaraBatchStats* s)
+{
+    if (!b || !s) return MARA_ERR_ARGUMENT;
+    std::memset(s, 0, sizeof(*s));
+    for (const auto& h : b->slots) {
+        if (!h.used) continue;
+        if (h.finished_reported) s->finished++;
+        else { s->active++; s->zones += h.zones; }
+    }
+    s->bytes_in_use = b->bytes_in_use;
+    s->zone_updates = b->zone_updates;
+    s->steps = b->step_count;
+    s->kernel_launches = b->launches;
+    return MARA_OK;
+}
+
+int mara_batch_tiles(MaraBatch* b, int* t1, int* t2)
+{
+    if (!b) return MARA_ERR_ARGUMENT;
+    if (t1) *t1 = b->tile1;
+    if (t2) *t2 = b->tile2;
+    return MARA_OK;
+}
+
+} // extern "C"

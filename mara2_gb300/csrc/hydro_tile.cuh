@@ -110,7 +110,8 @@ __device__ __forceinline__ void block_min_to(unsigned long long* dst, float v)
 //   grid's rotation holds U0 (read per zone); b, omb = b, 1 - b.
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict__ grids,
-                                                        const TileRef* __restrict__ tiles, int ntiles,
+                                                        const TileRef* __restrict__ tiles,
+                                                        const int* __restrict__ ntiles_p,
                                                         const int* __restrict__ rot,  // per grid: state buffer s
                                                         const double* __restrict__ dtg, int dt_stride,
                                                         const int* __restrict__ done, int done_stride,
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
     __shared__ float Fx[5][TY][TX + 1];
     __shared__ float Fy[5][DIM == 2 ? TY + 1 : 1][TX];
 
+    const int ntiles = *ntiles_p;  // device-resident so a captured graph follows a changing tile list
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const TileRef tr = tiles[t];
         const HGrid& g = grids[tr.grid];

@@ -362,6 +362,7 @@ struct MixedState {
     HGrid* dgrid = nullptr;
     TileRef* dtiles = nullptr;
     int ntiles = 0;
+    int* dntiles = nullptr;
     int* drot = nullptr;     // state buffer index (device)
     int rot = 0;             // host mirror for the general form's parity
     unsigned long long* dcfl = nullptr;
@@ -442,6 +443,8 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
             for (int x = 0; x < G.n[0]; x += m->tx) tiles.push_back({0, x, y, 0});
         m->ntiles = (int) tiles.size();
         rc = dev_alloc((void**) &m->dgrid, sizeof(HGrid), s, bytes);
+        if (!rc) rc = dev_alloc((void**) &m->dntiles, sizeof(int), s, bytes);
+        if (!rc) cudaMemcpyAsync(m->dntiles, &m->ntiles, sizeof(int), cudaMemcpyHostToDevice, s);
         if (!rc) rc = dev_alloc((void**) &m->dtiles, sizeof(TileRef) * tiles.size(), s, bytes);
         if (!rc) {
             cudaMemcpyAsync(m->dgrid, &h, sizeof(HGrid), cudaMemcpyHostToDevice, s);
@@ -468,6 +471,7 @@ void mixed_destroy(MixedState* m)
     for (int a = 0; a < 3; ++a) cudaFree(m->F[a]);
     cudaFree(m->dgrid);
     cudaFree(m->dtiles);
+    cudaFree(m->dntiles);
     delete m;
 }
 
@@ -624,7 +628,7 @@ static void tile_launch(MixedState* m, const double* dt, DevStatus* st, cudaStre
 {
     constexpr int TX = DIM == 2 ? 32 : 256, TY = DIM == 2 ? 16 : 1, NT = 256;
     hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT><<<m->ctas, NT, 0, s>>>(
-        m->dgrid, m->dtiles, m->ntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+        m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
 }
 
 template <int DIM>

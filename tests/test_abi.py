@@ -13,18 +13,24 @@ def _declared(header):
     return sorted(set(re.findall(r"\b(mara_gpu_\w+)\s*\(", text)))
 
 
+def _declared_batch():
+    text = open(os.path.join(ROOT, "include", "mara_batch.h")).read()
+    return sorted(set(re.findall(r"\b(mara_batch_\w+)\s*\(", text)))
+
+
 def test_header_declarations_are_bound():
-    from mara2_gb300 import _native as N
+    from mara2_gb300 import _native as N, batch as B
     declared = _declared("mara_gpu.h")
     assert declared, "no declarations found"
     assert sorted(N.SIGNATURES) == declared
+    assert sorted(B.SIGNATURES) == _declared_batch()
 
 
 def test_library_exports_every_declared_symbol():
     from mara2_gb300 import build, _native as N
     build.build()
     lib = N.load()
-    for name in _declared("mara_gpu.h"):
+    for name in _declared("mara_gpu.h") + _declared_batch():
         assert hasattr(lib, name), name
 
 
