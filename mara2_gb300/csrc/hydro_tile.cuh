@@ -140,33 +140,70 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
         else { src = (s + 2) % 3; dst = s; }
         const float* __restrict__ Uin = g.Uh[src];
 
+        // L2 prefetch of what the update phase reads per zone besides the
+        // stage input's high word (already staged below): its low word and,
+        // after the first stage, both words of U0
+        {
+            const int rows = DIM == 2 ? TY : 1;
+            const int per = (TX * 4 + 127) / 128;            // 128-byte lines per row segment
+            const int arrays = stage == 0 ? 1 : 3;
+            const int lines = arrays * 5 * rows * per;
+            for (int l = threadIdx.x; l < lines; l += NT) {
+                const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
+                const int y = tr.y0 + r, x = tr.x0 + seg * 32;
+                if (y < g.n1 && x < g.n0) {
+                    const float* base = a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
+                    const float* ptr = base + q * g.sU + (long long) y * g.n0 + x;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+                }
+            }
+        }
+
         __syncthreads(); // the previous tile's shared data is consumed
-        // 1. primitives of the tile and its halo
-        for (int c = threadIdx.x; c < WX * WY; c += NT) {
-            const int lx = c % WX, ly = c / WX;
-            int flipx = 0, flipy = 0;
-            const int x = bc_image(tr.x0 + lx - G, g.n0, g.bc, flipx);
-            const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, g.n1, g.bc, flipy) : 0;
-            const long long o = (long long) y * g.n0 + x;
-            float U[5];
+        // 1. primitives of the tile and its halo: all loads first, then the
+        //    conversions, so each thread keeps NC x 5 loads in flight
+        {
+            constexpr int NC = (WX * WY + NT - 1) / NT;
+            float Ur[NC][5];
+            int fl[NC];
 #pragma unroll
-            for (int q = 0; q < 5; ++q) U[q] = Uin[q * g.sU + o];
-            if (flipx) U[1] = -U[1];
-            if (flipy) U[2] = -U[2];
-            float P[5];
-            hydro_cons_f(g.gamma, U, P);
+            for (int k = 0; k < NC; ++k) {
+                const int c = threadIdx.x + k * NT;
+                fl[k] = 0;
+                if (c < WX * WY) {
+                    const int lx = c % WX, ly = c / WX;
+                    int flipx = 0, flipy = 0;
+                    const int x = bc_image(tr.x0 + lx - G, g.n0, g.bc, flipx);
+                    const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, g.n1, g.bc, flipy) : 0;
+                    const long long o = (long long) y * g.n0 + x;
 #pragma unroll
-            for (int q = 0; q < 5; ++q) Ps[q][ly][lx] = P[q];
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = Uin[q * g.sU + o];
+                    fl[k] = flipx | (flipy << 1);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const int c = threadIdx.x + k * NT;
+                if (c < WX * WY) {
+                    const int lx = c % WX, ly = c / WX;
+                    if (fl[k] & 1) Ur[k][1] = -Ur[k][1];
+                    if (fl[k] & 2) Ur[k][2] = -Ur[k][2];
+                    float P[5];
+                    hydro_cons_f(g.gamma, Ur[k], P);
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) Ps[q][ly][lx] = P[q];
+                }
+            }
         }
         __syncthreads();
 
-        // 2. x faces (face fx sits left of tile zone fx)
-        {
-            const float nx[3] = {1.f, 0.f, 0.f};
-            for (int f = threadIdx.x; f < FXN; f += NT) {
+        // 2. x faces and y faces in one balanced loop (face fx sits left of
+        //    tile zone fx, face fy below tile row fy)
+        for (int f = threadIdx.x; f < FXN + (DIM == 2 ? FYN : 0); f += NT) {
+            float PL[5], PR[5], Fh[5];
+            if (f < FXN) {
                 const int fx = f % (TX + 1), fy = f / (TX + 1);
                 const int ry = DIM == 2 ? fy + G : 0;
-                float PL[5], PR[5];
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
                     float v[2 * G];
@@ -174,18 +211,13 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
                     for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][ry][fx + m];
                     recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
                 }
-                float Fh[5];
+                const float nx[3] = {1.f, 0.f, 0.f};
                 hydro_face_flux<RIEMANN>(g.gamma, PL, PR, nx, Fh);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Fx[q][fy][fx] = Fh[q];
-            }
-        }
-        // y faces
-        if constexpr (DIM == 2) {
-            const float ny[3] = {0.f, 1.f, 0.f};
-            for (int f = threadIdx.x; f < FYN; f += NT) {
-                const int fx = f % TX, fy = f / TX;
-                float PL[5], PR[5];
+            } else if constexpr (DIM == 2) {
+                const int h = f - FXN;
+                const int fx = h % TX, fy = h / TX;
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
                     float v[2 * G];
@@ -193,7 +225,7 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
                     for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][fy + m][fx + G];
                     recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
                 }
-                float Fh[5];
+                const float ny[3] = {0.f, 1.f, 0.f};
                 hydro_face_flux<RIEMANN>(g.gamma, PL, PR, ny, Fh);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Fy[q][fy][fx] = Fh[q];

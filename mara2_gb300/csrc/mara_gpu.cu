@@ -499,7 +499,16 @@ int mara_gpu_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final, do
     CK(cudaSetDevice(h->cfg.device));
     k_run_begin<<<1, 1, 0, h->stream>>>(h->st, *t);
     h->launches++;
-    int rc = enqueue_run(h, max_steps, cfl, t_final);
+    // with an end time, look at the device's done flag every 64 steps so the
+    // host stops enqueuing once the run has reached t_final
+    const int chunk = t_final >= 0.0 ? 64 : max_steps;
+    int rc = MARA_OK;
+    for (int left = max_steps; left > 0 && rc == MARA_OK; left -= chunk) {
+        rc = enqueue_run(h, left < chunk ? left : chunk, cfl, t_final);
+        if (rc || left <= chunk || t_final < 0.0) break;
+        rc = read_status(h);
+        if (rc || h->st_host->done) break;
+    }
     if (rc) return rc;
     rc = read_status(h);
     *t = h->st_host->t;

@@ -73,6 +73,10 @@ __device__ __forceinline__ df rk_combine(df U0, df U, float dtL, float b, float 
 {
     const df s = df_add_f(U, dtL);
     if (one_minus_b == 0.0f) return s;
+    if (b == 0.5f) {  // (U0 + s) / 2: halving is exact on both words
+        const df t = df_add(U0, s);
+        return {0.5f * t.hi, 0.5f * t.lo};
+    }
     return df_add(df_mul_f(U0, one_minus_b), df_mul_f(s, b));
 }
 
@@ -80,18 +84,18 @@ __device__ __forceinline__ df rk_combine(df U0, df U, float dtL, float b, float 
 __device__ __forceinline__ float fmin3(float a, float b, float c) { return fminf(a, fminf(b, c)); }
 __device__ __forceinline__ float fmax3(float a, float b, float c) { return fmaxf(a, fmaxf(b, c)); }
 
-// generalized minmod of Reconstruction.cpp:55-61
+// generalized minmod of Reconstruction.cpp:55-61.  With a = theta (u0 - ul),
+// b = (ur - ul) / 2, c = theta (ur - u0), the reference's
+// 0.25 |sgn a + sgn b| (sgn a + sgn c) min(|a|, |b|, |c|) is non-zero only
+// when a and c share a sign (b is then a positive combination of the same
+// two differences and shares it too), and then equals sgn(a) min(|a|,|b|,|c|).
 __device__ __forceinline__ float minmod_f(float theta, float ul, float u0, float ur)
 {
     const float a = theta * (u0 - ul);
     const float b = 0.5f * (ur - ul);
     const float c = theta * (ur - u0);
     const float m = fmin3(fabsf(a), fabsf(b), fabsf(c));
-    // 0.25 |sgn a + sgn b| (sgn a + sgn c) min(|a|,|b|,|c|): non-zero only
-    // when a, b, c share a sign, and then it is sgn(a) * min
-    const bool pos = (a > 0.f) & (b > 0.f) & (c > 0.f);
-    const bool neg = (a < 0.f) & (b < 0.f) & (c < 0.f);
-    return pos ? m : (neg ? -m : 0.0f);
+    return a * c > 0.0f ? copysignf(m, a) : 0.0f;
 }
 
 // WENO5 point value at the right / left edge (Reconstruction.cpp:68-169)
