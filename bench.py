@@ -259,6 +259,101 @@ def cpu_baseline(s, P0, budget_s: float = 20.0):
                       f"(oracle C restatement, OpenMP, {threads} threads)"}
 
 
+def _l1_rho(a, b, s):
+    pa, pb = a[s.interior()], b[s.interior()]
+    return float(np.sum(np.abs(pb[..., 0] - pa[..., 0])) / np.sum(np.abs(pa[..., 0])))
+
+
+def _rate(g, s, steps, t_final=None):
+    """Zone-updates/s of `steps` device-resident steps (host wall clock around
+    a synchronising run; the first Courant step is computed beforehand)."""
+    import torch
+    g.run(1, s.cfl, t_final)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = g.run(steps, s.cfl, t_final)
+    el = time.perf_counter() - t0
+    return s.zones * n / el, n, el
+
+
+def workload_suite(device: int, serving_requests: int = 512):
+    """The other benchmark workloads, each on both precisions."""
+    from mara2_gb300 import workloads as W
+    from mara2_gb300.batch import autotune, serve
+    from mara2_gb300.solver import Solver
+    out = {}
+
+    # 1. Sod shock tube, 1024 zones, to t = 0.2 (whole run)
+    s, P0 = W.sod(1024)
+    res = {}
+    for prec in ("mixed", "fp64"):
+        with Solver(s, prec, device) as g:
+            g.upload(P0.copy())
+            t0 = time.perf_counter()
+            n = g.run(100_000, s.cfl, s.t_final)
+            el = time.perf_counter() - t0
+            res[prec] = (g.download(), n, el)
+    out["sod_1024_t0.2"] = {
+        "mixed_zone_updates_per_s": s.zones * res["mixed"][1] / res["mixed"][2],
+        "plain_fp64_zone_updates_per_s": s.zones * res["fp64"][1] / res["fp64"][2],
+        "steps_mixed": res["mixed"][1], "steps_fp64": res["fp64"][1],
+        "l1_density_vs_fp64_at_t_final": _l1_rho(res["fp64"][0], res["mixed"][0], s),
+        "note": "launch-bound: 1024 zones per step"}
+
+    # 3. 3-D MHD turbulence with CT, 256^3, RK3
+    s, P0 = W.mhd_turbulence(256)
+    dx = 1.0 / 256
+    bmax = float(np.abs(P0[..., 5:8]).max())
+    entry = {}
+    with Solver(s, "mixed", device) as g:
+        g.upload(P0.copy())
+        entry["mixed_zone_updates_per_s"], n, _ = _rate(g, s, 6)
+        entry["mixed_max_div_b_dx_over_bmax"] = g.monopole_max(dx) * dx / bmax
+    with Solver(s, "fp64", device) as g:
+        g.upload(P0.copy())
+        entry["plain_fp64_zone_updates_per_s"], n, _ = _rate(g, s, 2)
+        entry["plain_max_div_b_dx_over_bmax"] = g.monopole_max(dx) * dx / bmax
+    with Solver(s, "fp64", device) as a, Solver(s, "mixed", device) as b:
+        a.upload(P0.copy())
+        b.upload(P0.copy())
+        for _ in range(3):
+            a.run(1)
+            b.advance(a.stats().last_dt)
+        entry["l1_density_vs_fp64_3_steps"] = _l1_rho(a.download(), b.download(), s)
+    out["mhd_ct_256cube_rk3"] = entry
+    del P0
+
+    # 4. relativistic MHD blast, 512^2, WENO5 + HLLE, RK3
+    s, P0 = W.rmhd_blast(512)
+    entry = {}
+    with Solver(s, "mixed", device) as g:
+        g.upload(P0.copy())
+        entry["mixed_zone_updates_per_s"], n, _ = _rate(g, s, 20)
+        entry["mixed_failures"] = g.stats().failures
+    with Solver(s, "fp64", device) as g:
+        g.upload(P0.copy())
+        entry["plain_fp64_zone_updates_per_s"], n, _ = _rate(g, s, 3)
+    with Solver(s, "fp64", device) as a, Solver(s, "mixed", device) as b:
+        a.upload(P0.copy())
+        b.upload(P0.copy())
+        for _ in range(10):
+            a.run(1)
+            b.advance(a.stats().last_dt)
+        entry["l1_density_vs_fp64_10_steps"] = _l1_rho(a.download(), b.download(), s)
+        entry["plain_failures"] = a.stats().failures
+    out["rmhd_blast_512_weno5_rk3"] = entry
+
+    # 5. serving: a bounded Poisson stream of Riemann problems
+    tiles = autotune(device)
+    reqs = W.riemann_stream(serving_requests, rate=2000.0)
+    r = serve(reqs, budget_bytes=32 << 30, tile_1d=tiles["tile_1d"], tile_2d=tiles["tile_2d"], device=device)
+    out["serving_riemann_stream"] = {**r.summary(), "requests_in_sample": serving_requests,
+                                     "stream": "1-D N log-uniform [256, 8192] / 2-D side log-uniform [128, 512], "
+                                               "Poisson 2000/s, t = 0.2, PLM + HLLC, RK2",
+                                     "tiles": {"tile_1d": tiles["tile_1d"], "tile_2d": tiles["tile_2d"]}}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -267,6 +362,8 @@ def main():
     ap.add_argument("--impl", default="mara2_gb300")
     ap.add_argument("--n", type=int, default=N_SIDE)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-workloads", action="store_true", help="skip the per-workload section")
+    ap.add_argument("--serving-requests", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -321,6 +418,7 @@ def main():
         gp.upload(P0.copy())
         ms_plain, _, _ = time_resident(gp, max(3, args.steps // 5), 3, local)
     l1_rho, linf_rho = l1_vs_fp64(s, P0, 20, local)
+    suite = None if args.no_workloads or rank != 0 else workload_suite(local, args.serving_requests)
 
     if rank != 0:
         return
@@ -342,6 +440,7 @@ def main():
         "cpu_baseline": cb,
         "clocks": clocks,
         "step_ms_min": min(ms_all), "step_ms_max": max(ms_all),
+        "workloads": suite,
     }
     print(json.dumps(line))
 

@@ -148,6 +148,12 @@ void* mara_gpu_stream(MaraGpuHandle* h);
 int mara_gpu_set_kernel_timing(MaraGpuHandle* h, int enable);
 int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches[3]);
 
+/* CellCenteredFieldCT::monopole (MeshLocation::cell, CellCenteredFieldCT.cpp:
+ * 159-223) of the resident magnetic field, reduced to the largest |div B| over
+ * the interior zones; mesh_spacing is CellCenteredFieldCT::setMeshSpacing
+ * (the reference's default is 1).  MHD and RMHD only. */
+int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs);
+
 /* Device bytes the handle holds. */
 int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
 

@@ -30,6 +30,7 @@ UNITS = {
     "batch.cu": ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "mara_gpu.cu": ["--fmad=false"],
     "no_alloc.cu": ["--fmad=false"],
+    "diagnostics.cu": ["--fmad=false"],
 }
 
 

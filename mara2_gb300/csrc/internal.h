@@ -54,6 +54,10 @@ void plain_update(int law, const GridDesc& G, const PhysParamsH& pp, const doubl
 void plain_courant(int law, const GridDesc& G, const PhysParamsH& pp, const double* P, DevStatus* st,
                    cudaStream_t s);
 
+// ---- diagnostics (diagnostics.cu) ----------------------------------------------
+void launch_monopole_max(const void* P, bool fp32, const GridDesc& G, double h, unsigned long long* out,
+                         cudaStream_t s);
+
 // ---- shared helpers (mara_gpu.cu) --------------------------------------------
 void launch_courant_init(DevStatus* st, cudaStream_t s);
 void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s);

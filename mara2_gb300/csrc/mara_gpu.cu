@@ -584,6 +584,24 @@ int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches
     return MARA_OK;
 }
 
+int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs)
+{
+    if (!h || !max_abs || !(mesh_spacing > 0.0)) return MARA_ERR_ARGUMENT;
+    if (h->cfg.law == MARA_LAW_HYDRO) return MARA_ERR_CONFIG;
+    CK(cudaSetDevice(h->cfg.device));
+    const void* P = h->mixed ? (const void*) mixed_primitives(h->mixed) : (const void*) h->P[h->cur];
+    if (!P) return MARA_ERR_CONFIG;
+    unsigned long long* out = &h->st->dt_bits;  // scratch word: the next Courant call re-initialises it
+    CK(cudaMemsetAsync(out, 0, sizeof(unsigned long long), h->stream));
+    launch_monopole_max(P, h->mixed != nullptr, h->G, mesh_spacing, out, h->stream);
+    h->launches++;
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, out, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *max_abs = __builtin_bit_cast(double, bits);
+    return MARA_OK;
+}
+
 int64_t mara_gpu_device_bytes(const MaraGpuHandle* h) { return h ? h->bytes : 0; }
 
 const char* mara_gpu_status_string(int s)

@@ -150,7 +150,7 @@ __device__ __forceinline__ int guard_images_m(int ii, int n, int g, int bc, int*
 // primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
 // ConsToPrimRMHD for RMHD (the Newton iteration keeps FP64)
 template <int LAW>
-__device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code)
+__device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code, const float* Pprev = nullptr)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     if constexpr (LAW == LAW_HYDRO) {
@@ -191,6 +191,19 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
         for (int q = 0; q < 8; ++q) s.Cons[q] = U[q];
         s.Z_start = sqrt(s.S2 + s.D * s.D);
         s.W_start = s.Z_start / s.D;
+        if (Pprev) {
+            // warm start from the zone's primitives of the previous stage
+            // (ConsToPrimRMHD::set_starting_prim, ConsToPrimRMHD.cpp:99-108):
+            // Z = rho h W^2 and W of the old state are close to the new root
+            const double rho = Pprev[0], pre = Pprev[4];
+            const double V2 = (double) Pprev[1] * Pprev[1] + (double) Pprev[2] * Pprev[2] + (double) Pprev[3] * Pprev[3];
+            if (rho > 0.0 && pre > 0.0 && V2 < 1.0) {
+                const double W2 = 1.0 / (1.0 - V2);
+                const double h = 1.0 + pre / (rho * (pp.gamma - 1.0)) + pre / rho;
+                s.Z_start = rho * h * W2;
+                s.W_start = sqrt(W2);
+            }
+        }
         int err = rm_anton2dzw(s, Pd);
         if (err != ST_OK) err = rm_noble1dw(s, Pd);
         if (err != ST_OK) { *code = err; return ST_INVERSION_FAILURE; }
@@ -231,14 +244,17 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
     float Pn[NQ];
     int code = ST_OK;
     const long long pc = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    const int e = recover_mixed<LAW>(G, Un, Pn, &code);
+    float Pold[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) Pold[q] = Pf[q * G.sP + pc];
+    const int e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
     if (e == ST_INVERSION_FAILURE) {
         atomicAdd(&st->failures, 1);
         const unsigned long long z = (unsigned long long) uc;
         const unsigned long long prev = atomicMin(&st->first_zone, z);
         if (z < prev) atomicExch(&st->first_code, code);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Pn[q] = Pf[q * G.sP + pc];
+        for (int q = 0; q < NQ; ++q) Pn[q] = Pold[q];
     }
     int ix[4], iy[4], iz[4], sx[4], sy[4], sz[4];
     const int cx = guard_images_m(ii, G.n[0], G.g[0], G.bc, ix, sx);
@@ -679,6 +695,7 @@ int mixed_parity(const MixedState* m) { return m->rot & 1; }
 void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
 void mixed_advance_parity(MixedState* m) { if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1; }
 void mixed_set_timing(MixedState* m, int on) { m->timing = on; }
+const float* mixed_primitives(const MixedState* m) { return m->Pf; }
 
 void mixed_kernel_times(MixedState* m, double ms[3], int64_t launches[3])
 {

@@ -23,5 +23,7 @@ void mixed_set_parity(MixedState* m, int p);
 void mixed_advance_parity(MixedState* m);
 void mixed_set_timing(MixedState* m, int on);
 void mixed_kernel_times(MixedState* m, double ms[3], int64_t launches[3]);
+// FP32 primitives with guards of the general form (nullptr for the fused form)
+const float* mixed_primitives(const MixedState* m);
 
 } // namespace mara

@@ -115,6 +115,13 @@ class Solver:
     def stream(self) -> int:
         return self.lib.mara_gpu_stream(self.h)
 
+    def monopole_max(self, mesh_spacing: float = 1.0) -> float:
+        """Largest |div B| (CellCenteredFieldCT::monopole at cells) over the
+        interior of the resident state."""
+        m = C.c_double()
+        N.check(self.lib.mara_gpu_monopole(self.h, mesh_spacing, C.byref(m)), "mara_gpu_monopole")
+        return m.value
+
     def device_bytes(self) -> int:
         return self.lib.mara_gpu_device_bytes(self.h)
 

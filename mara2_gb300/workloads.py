@@ -137,13 +137,28 @@ def _fourier_modes(seed: int, kmax: int = 4):
 
 def _fourier_vector(seed, X, Y, Z, kmax=4):
     """Sum over modes 0 < |k| <= kmax of a random-amplitude, random-phase
-    vector wave; returns (3, *X.shape)."""
+    vector wave, amp_k cos(2 pi (k.x + phi_k)), on the tensor-product grid
+    X, Y, Z (meshgrid, 'ij'); returns (3, *X.shape).  Evaluated as a
+    separable inverse DFT: cos(2 pi (k.x + phi)) = Re e^{2 pi i phi}
+    e^{2 pi i kx x} e^{2 pi i ky y} e^{2 pi i kz z}, contracted one axis at a
+    time over the 2 kmax + 1 wavenumbers per axis."""
     ks, r = _fourier_modes(seed, kmax)
-    out = np.zeros((3,) + X.shape)
+    K = 2 * kmax + 1
+    C = np.zeros((3, K, K, K), dtype=np.complex128)
     for m, k in enumerate(ks):
-        phase = 2 * math.pi * (k[0] * X + k[1] * Y + k[2] * Z) + 2 * math.pi * r[m, 3]
         amp = (r[m, :3] - 0.5) / max(1.0, float(np.dot(k, k)))
-        out += amp[:, None, None, None] * np.cos(phase)[None]
+        a, b, c = (int(v) + kmax for v in k)
+        C[:, a, b, c] += amp * np.exp(2j * math.pi * r[m, 3])
+    wav = np.arange(-kmax, kmax + 1, dtype=np.float64)
+    x, y, z = X[:, 0, 0], Y[0, :, 0], Z[0, 0, :]
+    ex = np.exp(2j * math.pi * np.outer(wav, x))
+    ey = np.exp(2j * math.pi * np.outer(wav, y))
+    ez = np.exp(2j * math.pi * np.outer(wav, z))
+    T = np.einsum("cabd,dk->cabk", C, ez)
+    T = np.einsum("cabk,bj->cajk", T, ey)
+    out = np.empty((3,) + X.shape)
+    for comp in range(3):
+        out[comp] = np.tensordot(ex, T[comp], axes=([0], [0])).real
     return out
 
 
