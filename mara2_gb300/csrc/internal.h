@@ -38,6 +38,9 @@ struct DevStatus {
     double t;                       // driver-loop time
     double dt;                      // dt of the current step
     long long steps;                // driver-loop steps taken
+    int halt;                       // a previous stage had inversion failures: the
+                                    // step stops there, as the reference's
+                                    // InversionFailure ends MethodOfLinesTVD::advance
 };
 
 struct PhysParamsH {

@@ -50,6 +50,14 @@ __global__ void k_advance_time(DevStatus* st)
     st->steps += 1;
 }
 
+__global__ void k_status_reset(DevStatus* st)
+{
+    DevStatus z;
+    memset(&z, 0, sizeof(z));
+    z.first_zone = ~0ull;
+    *st = z;
+}
+
 __global__ void k_run_begin(DevStatus* st, double t)
 {
     st->t = t;
@@ -376,6 +384,10 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    // a new state starts with a clean status (errors of the previous state
+    // are reported until then)
+    k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+    h->launches++;
     const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
     CK(cudaMemcpyAsync(h->stage_aos, P_aos, bytes, cudaMemcpyHostToDevice, h->stream));
     if (h->mixed) mixed_load_aos(h->mixed, h->stage_aos, h->st, h->stream);

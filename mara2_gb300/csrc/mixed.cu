@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     constexpr int S = SOf<RECON>::S;
-    if (*done || st->code || st->failures) return;
+    if (*done || st->code) return;
+    if (st->failures) { st->halt = 1; return; }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nb0) return;
     const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
                                                        const int* __restrict__ done, DevStatus* st)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    if (*done || st->code || st->failures) return;
+    if (*done || st->code || st->halt) return;
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= G.n[0]) return;
     const int jj = blockIdx.y, kk = blockIdx.z;

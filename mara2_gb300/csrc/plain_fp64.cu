@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(128) flux_kernel(const double* __restrict__ P,
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     constexpr int S = ReconInfo<RECON>::S;
-    if (st->code != 0 || st->failures != 0 || st->done) return;
+    if (st->code != 0 || st->done) return;
+    if (st->failures != 0) { st->halt = 1; return; }  // failures are final once the stage ended
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nb0) return;
     const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ 
                                                      const double* __restrict__ dtp, DevStatus* __restrict__ st)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    if (st->code != 0 || st->failures != 0 || st->done) return;
+    if (st->code != 0 || st->halt || st->done) return;
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= G.n[0]) return;
     const int jj = blockIdx.y, kk = blockIdx.z;
