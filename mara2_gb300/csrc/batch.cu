@@ -89,7 +89,7 @@ __global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v;
 
 // host FP64 primitives (AoS with guards) -> FP32-pair conserved state of one
 // slot, and the grid's first Courant step
-__global__ void k_batch_load(const double* __restrict__ aos, HGrid g, int g0, int g1, int N0, int N1, double gamma,
+__global__ void k_batch_load(const double* __restrict__ aos, HGrid g, int g0, int g1, int N0, int N1, double inv_gm1,
                              unsigned long long* cflbit)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -99,13 +99,7 @@ __global__ void k_batch_load(const double* __restrict__ aos, HGrid g, int g0, in
         double P[5], U[5];
 #pragma unroll
         for (int q = 0; q < 5; ++q) P[q] = aos[c * 5 + q];
-        const double gm1 = gamma - 1.0;
-        const double vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
-        U[0] = P[0];
-        U[1] = P[0] * P[1];
-        U[2] = P[0] * P[2];
-        U[3] = P[0] * P[3];
-        U[4] = P[0] * 0.5 * vv + P[4] / gm1;
+        hydro_p2u_d(P, inv_gm1, U);
         const long long o = (long long) y * g.n0 + x;
         float Uf[5];
 #pragma unroll
@@ -115,7 +109,7 @@ __global__ void k_batch_load(const double* __restrict__ aos, HGrid g, int g0, in
             g.Ul[0][q * g.sU + o] = d.lo;
             Uf[q] = d.hi;
         }
-        zdt = hydro_zone_dt(g, Uf);
+        zdt = hydro_zone_dt(g.gamma, g.lmin, Uf);
     }
     block_min_to(cflbit, zdt);
 }
@@ -134,14 +128,8 @@ __global__ void k_batch_store(HGrid g, int buf, int g0, int g1, int N0, int N1, 
     double U[5];
 #pragma unroll
     for (int q = 0; q < 5; ++q) U[q] = (double) g.Uh[buf][q * g.sU + o] + (double) g.Ul[buf][q * g.sU + o];
-    const double gm1 = gamma - 1.0;
-    const double pp = U[1] * U[1] + U[2] * U[2] + U[3] * U[3];
     double P[5];
-    P[0] = U[0];
-    P[4] = (U[4] - 0.5 * pp / U[0]) * gm1;
-    P[1] = U[1] / U[0];
-    P[2] = U[2] / U[0];
-    P[3] = U[3] / U[0];
+    hydro_u2p_d(U, gamma - 1.0, P);
     if (fx) P[1] = -P[1];
     if (fy) P[2] = -P[2];
 #pragma unroll
@@ -435,7 +423,8 @@ int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* c, const double* P_aos, 
                                         t_final, cfl);
     k_set_u64<<<1, 1, 0, b->stream>>>(b->cflbits + sl, ~0ull);
     dim3 grid((c->ni + 255) / 256, c->nj);
-    k_batch_load<<<grid, 256, 0, b->stream>>>(b->staging, g, h.g0, h.g1, N0, N1, c->gamma, b->cflbits + sl);
+    k_batch_load<<<grid, 256, 0, b->stream>>>(b->staging, g, h.g0, h.g1, N0, N1, 1.0 / (c->gamma - 1.0),
+                                              b->cflbits + sl);
     b->launches += 3;
     b->done_host[sl] = 0;
     b->dirty = true;

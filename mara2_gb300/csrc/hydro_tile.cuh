@@ -57,6 +57,31 @@ __device__ __forceinline__ int bc_image(int x, int n, int bc, int& flip)
     return x < 0 ? 0 : (x >= n ? n - 1 : x);
 }
 
+// Hydro primitive <-> conserved conversion in double precision at the host
+// boundary of the mixed-precision forms.  Every operation is rounded on its
+// own (no multiply-add contraction), so the single-grid and the batched
+// loaders and stores produce the same bits from the same primitives.
+__device__ __forceinline__ void hydro_p2u_d(const double* P, double inv_gm1, double* U)
+{
+    const double vv = __dadd_rn(__dadd_rn(__dmul_rn(P[1], P[1]), __dmul_rn(P[2], P[2])), __dmul_rn(P[3], P[3]));
+    U[0] = P[0];
+    U[1] = __dmul_rn(P[0], P[1]);
+    U[2] = __dmul_rn(P[0], P[2]);
+    U[3] = __dmul_rn(P[0], P[3]);
+    U[4] = __dadd_rn(__dmul_rn(__dmul_rn(0.5, P[0]), vv), __dmul_rn(P[4], inv_gm1));
+}
+
+__device__ __forceinline__ void hydro_u2p_d(const double* U, double gm1, double* P)
+{
+    const double ir = 1.0 / U[0];
+    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(U[1], U[1]), __dmul_rn(U[2], U[2])), __dmul_rn(U[3], U[3]));
+    P[0] = U[0];
+    P[1] = __dmul_rn(U[1], ir);
+    P[2] = __dmul_rn(U[2], ir);
+    P[3] = __dmul_rn(U[3], ir);
+    P[4] = __dmul_rn(__dsub_rn(U[4], __dmul_rn(__dmul_rn(0.5, pp), ir)), gm1);
+}
+
 template <int RECON> struct HaloOf { static constexpr int G = RECON == RECON_PCM ? 1 : 2; };
 
 template <int RECON>
@@ -84,14 +109,16 @@ __device__ __forceinline__ void hydro_face_flux(float gamma, const float* PL, co
 
 // Courant step of one zone: lmin / max over x, y, z of max |eigenvalue|
 // (FieldOperator::getCourantTimestep); for hydro max |A| = max|v_a| + cs.
-__device__ __forceinline__ float hydro_zone_dt(const HGrid& g, const float* U)
+__device__ __forceinline__ float hydro_zone_dt(float gamma, float lmin, const float* U)
 {
     float P[5];
-    hydro_cons_f(g.gamma, U, P);
-    const float cs = sqrtf(g.gamma * P[4] / P[0]);
+    hydro_cons_f(gamma, U, P);
+    const float cs = sqrtf(gamma * P[4] / P[0]);
     const float vmax = fmaxf(fabsf(P[1]), fmaxf(fabsf(P[2]), fabsf(P[3])));
-    return g.lmin / (vmax + cs);
+    return lmin / (vmax + cs);
 }
+
+__device__ __forceinline__ float hydro_zone_dt(const HGrid& g, const float* U) { return hydro_zone_dt(g.gamma, g.lmin, U); }
 
 __device__ __forceinline__ void block_min_to(unsigned long long* dst, float v)
 {

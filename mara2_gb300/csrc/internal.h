@@ -67,6 +67,10 @@ void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStrea
 void launch_set_dt(DevStatus* st, double dt, cudaStream_t s);
 void launch_advance_time(DevStatus* st, cudaStream_t s);
 void launch_aos_to_soa(const double* aos, double* soa, const GridDesc& G, cudaStream_t s);
+void launch_aos_to_soa_range(const double* aos, double* soa, const GridDesc& G, long long c0, long long c1,
+                             cudaStream_t s);
+void launch_soa_to_aos_range(const double* soa, double* aos, const GridDesc& G, long long c0, long long c1,
+                             cudaStream_t s);
 void launch_soa_to_aos(const double* soa, double* aos, const GridDesc& G, cudaStream_t s);
 
 } // namespace mara

@@ -65,12 +65,13 @@ __global__ void k_run_begin(DevStatus* st, double t)
     st->done = 0;
 }
 
-// AoS (i, j, k, q), q fastest  <->  SoA q * sP + (k * N1 + j) * N0 + i
-__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, GridDesc G)
+// AoS (i, j, k, q), q fastest  <->  SoA q * sP + (k * N1 + j) * N0 + i, over
+// the AoS cells [c0, c1)
+__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, GridDesc G, long long c0,
+                             long long c1)
 {
-    const long long cells = G.sP;
-    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; // AoS cell order
-    if (c >= cells) return;
+    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x; // AoS cell order
+    if (c >= c1) return;
     const int k = (int) (c % G.N[2]);
     const int j = (int) ((c / G.N[2]) % G.N[1]);
     const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
@@ -78,11 +79,11 @@ __global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict_
     for (int q = 0; q < G.nq; ++q) soa[q * G.sP + s] = aos[c * G.nq + q];
 }
 
-__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos, GridDesc G)
+__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos, GridDesc G, long long c0,
+                             long long c1)
 {
-    const long long cells = G.sP;
-    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= cells) return;
+    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     const int k = (int) (c % G.N[2]);
     const int j = (int) ((c / G.N[2]) % G.N[1]);
     const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
@@ -97,15 +98,25 @@ void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStrea
 }
 void launch_set_dt(DevStatus* st, double dt, cudaStream_t s) { k_set_dt<<<1, 1, 0, s>>>(st, dt); }
 void launch_advance_time(DevStatus* st, cudaStream_t s) { k_advance_time<<<1, 1, 0, s>>>(st); }
+void launch_aos_to_soa_range(const double* aos, double* soa, const GridDesc& G, long long c0, long long c1,
+                             cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    k_aos_to_soa<<<(unsigned) ((c1 - c0 + 255) / 256), 256, 0, s>>>(aos, soa, G, c0, c1);
+}
+void launch_soa_to_aos_range(const double* soa, double* aos, const GridDesc& G, long long c0, long long c1,
+                             cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    k_soa_to_aos<<<(unsigned) ((c1 - c0 + 255) / 256), 256, 0, s>>>(soa, aos, G, c0, c1);
+}
 void launch_aos_to_soa(const double* aos, double* soa, const GridDesc& G, cudaStream_t s)
 {
-    const long long n = G.sP;
-    k_aos_to_soa<<<(unsigned) ((n + 255) / 256), 256, 0, s>>>(aos, soa, G);
+    launch_aos_to_soa_range(aos, soa, G, 0, G.sP, s);
 }
 void launch_soa_to_aos(const double* soa, double* aos, const GridDesc& G, cudaStream_t s)
 {
-    const long long n = G.sP;
-    k_soa_to_aos<<<(unsigned) ((n + 255) / 256), 256, 0, s>>>(soa, aos, G);
+    launch_soa_to_aos_range(soa, aos, G, 0, G.sP, s);
 }
 
 } // namespace mara
@@ -121,6 +132,8 @@ struct MaraGpuHandle {
     GridDesc G;
     PhysParamsH pp;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;          // host <-> device copies, overlapped with conversions
+    cudaEvent_t ev[17] = {};             // per-chunk events, [16] joins the streams
     double* P[2] = {nullptr, nullptr};  // primitive state with guards (plain path)
     int cur = 0;
     double* U0 = nullptr;
@@ -336,6 +349,9 @@ int mara_gpu_create(const MaraGpuConfig* config, MaraGpuHandle** out)
     h->pp.weno_is = config->weno_is;
     int rc = MARA_OK;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return MARA_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking) != cudaSuccess) rc = MARA_ERR_CUDA;
+    for (int e = 0; e < 17 && !rc; ++e)
+        if (cudaEventCreateWithFlags(&h->ev[e], cudaEventDisableTiming) != cudaSuccess) rc = MARA_ERR_CUDA;
     if (cudaMallocHost((void**) &h->st_host, sizeof(DevStatus)) != cudaSuccess) rc = MARA_ERR_CUDA;
     const GridDesc& G = h->G;
     const size_t pbytes = sizeof(double) * (size_t) G.sP * G.nq;
@@ -375,9 +391,21 @@ int mara_gpu_destroy(MaraGpuHandle* h)
     cudaFree(h->st);
     if (h->mixed) mixed_destroy(h->mixed);
     if (h->st_host) cudaFreeHost(h->st_host);
+    for (int e = 0; e < 17; ++e) if (h->ev[e]) cudaEventDestroy(h->ev[e]);
+    if (h->aux) cudaStreamDestroy(h->aux);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return MARA_OK;
+}
+
+// Transfers are split into chunks of whole cells: the copy of chunk k+1 (on
+// the auxiliary stream) overlaps the layout conversion of chunk k (on the
+// handle's stream).
+static int chunks_of(const MaraGpuHandle* h)
+{
+    const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
+    if (bytes < (size_t(4) << 20)) return 1;
+    return 8;
 }
 
 int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
@@ -388,11 +416,22 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
     // are reported until then)
     k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
     h->launches++;
-    const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
-    CK(cudaMemcpyAsync(h->stage_aos, P_aos, bytes, cudaMemcpyHostToDevice, h->stream));
-    if (h->mixed) mixed_load_aos(h->mixed, h->stage_aos, h->st, h->stream);
-    else launch_aos_to_soa(h->stage_aos, h->P[h->cur], h->G, h->stream);
-    h->launches++;
+    if (h->mixed) mixed_load_begin(h->mixed, h->stream);
+    const int C = chunks_of(h);
+    const long long cells = h->G.sP, nq = h->G.nq;
+    CK(cudaEventRecord(h->ev[16], h->stream));
+    CK(cudaStreamWaitEvent(h->aux, h->ev[16], 0));
+    for (int k = 0; k < C; ++k) {
+        const long long c0 = cells * k / C, c1 = cells * (k + 1) / C;
+        CK(cudaMemcpyAsync(h->stage_aos + c0 * nq, P_aos + c0 * nq, sizeof(double) * (c1 - c0) * nq,
+                           cudaMemcpyHostToDevice, h->aux));
+        CK(cudaEventRecord(h->ev[k], h->aux));
+        CK(cudaStreamWaitEvent(h->stream, h->ev[k], 0));
+        if (h->mixed) mixed_load_aos_range(h->mixed, h->stage_aos, c0, c1, h->st, h->stream);
+        else launch_aos_to_soa_range(h->stage_aos, h->P[h->cur], h->G, c0, c1, h->stream);
+        h->launches++;
+    }
+    if (h->mixed) mixed_load_finish(h->mixed, h->st, h->stream);
     return cuda_status(cudaGetLastError());
 }
 
@@ -400,11 +439,20 @@ int mara_gpu_download(MaraGpuHandle* h, double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
-    const size_t bytes = sizeof(double) * (size_t) h->G.sP * h->G.nq;
-    if (h->mixed) mixed_store_aos(h->mixed, h->stage_aos, h->stream);
-    else launch_soa_to_aos(h->P[h->cur], h->stage_aos, h->G, h->stream);
-    h->launches++;
-    CK(cudaMemcpyAsync(P_aos, h->stage_aos, bytes, cudaMemcpyDeviceToHost, h->stream));
+    const int C = chunks_of(h);
+    const long long cells = h->G.sP, nq = h->G.nq;
+    for (int k = 0; k < C; ++k) {
+        const long long c0 = cells * k / C, c1 = cells * (k + 1) / C;
+        if (h->mixed) mixed_store_aos_range(h->mixed, h->stage_aos, c0, c1, h->stream);
+        else launch_soa_to_aos_range(h->P[h->cur], h->stage_aos, h->G, c0, c1, h->stream);
+        h->launches++;
+        CK(cudaEventRecord(h->ev[k], h->stream));
+        CK(cudaStreamWaitEvent(h->aux, h->ev[k], 0));
+        CK(cudaMemcpyAsync(P_aos + c0 * nq, h->stage_aos + c0 * nq, sizeof(double) * (c1 - c0) * nq,
+                           cudaMemcpyDeviceToHost, h->aux));
+    }
+    CK(cudaEventRecord(h->ev[16], h->aux));
+    CK(cudaStreamWaitEvent(h->stream, h->ev[16], 0));
     CK(cudaStreamSynchronize(h->stream));
     return MARA_OK;
 }

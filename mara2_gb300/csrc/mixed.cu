@@ -32,6 +32,7 @@ struct GridF {
     float gamma, plm_theta, shenzha_A, pressure_floor;
     int weno_is;
     double gamma_d, pfloor_d;
+    double gm1_d, inv_gm1_d;
 };
 
 template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 1 : RECON == RECON_PLM ? 2 : 3; };
@@ -298,47 +299,64 @@ __global__ void __launch_bounds__(256) courant_f_kernel(const float* __restrict_
     block_min_to(dst, zdt);
 }
 
-// AoS FP64 MeshData::P -> FP32-pair conserved state (FP64 fromPrimitive)
-// and FP32 primitives with guards
+// AoS FP64 MeshData::P (cells [c0, c1)) -> FP32-pair conserved state and,
+// on the general form, FP32 primitives with guards.  Hydro converts with one
+// reciprocal instead of FP64 divisions (FP64 is slow on this GPU) and, when
+// cfl is given, reduces the Courant step of the loaded zones on the way.
 template <int LAW>
-__global__ void load_kernel(const double* __restrict__ aos, float* Uh, float* Ul, float* Pf, GridF G, PhysParams pp,
-                            DevStatus* st)
+__global__ void load_kernel(const double* __restrict__ aos, long long c0, long long c1, float* Uh, float* Ul,
+                            float* Pf, GridF G, PhysParams pp, DevStatus* st, unsigned long long* cfl)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= G.sP) return;
-    const int k = (int) (c % G.N[2]);
-    const int j = (int) ((c / G.N[2]) % G.N[1]);
-    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
-    double P[NQ];
+    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    float zdt = 3.0e38f;
+    if (c < c1) {
+        const int k = (int) (c % G.N[2]);
+        const int j = (int) ((c / G.N[2]) % G.N[1]);
+        const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+        double P[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) P[q] = aos[c * NQ + q];
-    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    if (Pf)
+        for (int q = 0; q < NQ; ++q) P[q] = aos[c * NQ + q];
+        const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
+        if (Pf)
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Pf[q * G.sP + s] = (float) P[q];
-    const int ii = i - G.g[0], jj = j - G.g[1], kk = k - G.g[2];
-    if (ii < 0 || jj < 0 || kk < 0 || ii >= G.n[0] || jj >= G.n[1] || kk >= G.n[2]) return;
-    double U[NQ];
-    const int e = law_p2u<LAW>(pp, P, U);
-    if (e != ST_OK) atomicCAS(&st->code, 0, e);
-    const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
+            for (int q = 0; q < NQ; ++q) Pf[q * G.sP + s] = (float) P[q];
+        const int ii = i - G.g[0], jj = j - G.g[1], kk = k - G.g[2];
+        if (ii >= 0 && jj >= 0 && kk >= 0 && ii < G.n[0] && jj < G.n[1] && kk < G.n[2]) {
+            double U[NQ];
+            if constexpr (LAW == LAW_HYDRO) {
+                hydro_p2u_d(P, G.inv_gm1_d, U);
+            } else {
+                const int e = law_p2u<LAW>(pp, P, U);
+                if (e != ST_OK) atomicCAS(&st->code, 0, e);
+            }
+            const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
+            float hi[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        const df d = df_from_double(U[q]);
-        Uh[q * G.sU + u] = d.hi;
-        Ul[q * G.sU + u] = d.lo;
+            for (int q = 0; q < NQ; ++q) {
+                const df d = df_from_double(U[q]);
+                Uh[q * G.sU + u] = d.hi;
+                Ul[q * G.sU + u] = d.lo;
+                hi[q] = d.hi;
+            }
+            // the Courant step from the stored high words, as the last RK
+            // stage computes it
+            if constexpr (LAW == LAW_HYDRO)
+                if (cfl) zdt = hydro_zone_dt(G.gamma, G.lmin, hi);
+        }
     }
+    if (cfl) block_min_to(cfl, zdt);
 }
 
-// FP32-pair state -> AoS FP64 primitives with guards (FP64 fromConserved of
-// each zone's boundary image)
+// FP32-pair state -> AoS FP64 primitives with guards (cells [c0, c1); the
+// guard zones are boundary images of interior zones)
 template <int LAW>
-__global__ void store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos, GridF G, PhysParams pp)
+__global__ void store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos, long long c0, long long c1,
+                             GridF G, PhysParams pp)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= G.sP) return;
+    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     const int k = (int) (c % G.N[2]);
     const int j = (int) ((c / G.N[2]) % G.N[1]);
     const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
@@ -350,8 +368,12 @@ __global__ void store_kernel(const float* Uh, const float* Ul, double* __restric
     double U[NQ], P[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) U[q] = (double) Uh[q * G.sU + u] + (double) Ul[q * G.sU + u];
-    int code = 0;
-    law_cons<LAW>(pp, U, P, &code);
+    if constexpr (LAW == LAW_HYDRO) {
+        hydro_u2p_d(U, G.gm1_d, P);
+    } else {
+        int code = 0;
+        law_cons<LAW>(pp, U, P, &code);
+    }
     if (f[0]) P[1] = -P[1];
     if (f[1]) P[2] = -P[2];
     if (f[2]) P[3] = -P[3];
@@ -417,6 +439,7 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
     F.gamma = (float) c->gamma; F.plm_theta = (float) c->plm_theta; F.shenzha_A = (float) c->shenzha_A;
     F.pressure_floor = (float) c->pressure_floor; F.weno_is = c->weno_is;
     F.gamma_d = c->gamma; F.pfloor_d = c->pressure_floor;
+    F.gm1_d = c->gamma - 1.0; F.inv_gm1_d = 1.0 / (c->gamma - 1.0);
     m->pp.gamma = c->gamma; m->pp.plm_theta = c->plm_theta; m->pp.shenzha_A = c->shenzha_A;
     m->pp.pressure_floor = c->pressure_floor; m->pp.weno_is = c->weno_is;
 
@@ -507,23 +530,6 @@ static void timed(MixedState* m, cudaStream_t s, Fn fn)
 
 static int host_rot(const MixedState* m) { return m->rot; }
 
-// Courant step straight from the FP32-pair state (fused hydro form)
-__global__ void __launch_bounds__(256) courant_u_kernel(const HGrid* __restrict__ grid, const int* __restrict__ rot,
-                                                        unsigned long long* __restrict__ dst)
-{
-    const HGrid& g = *grid;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-    float zdt = 3.0e38f;
-    if (x < g.n0) {
-        const long long o = (long long) y * g.n0 + x;
-        float U[5];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) U[q] = g.Uh[*rot][q * g.sU + o];
-        zdt = hydro_zone_dt(g, U);
-    }
-    block_min_to(dst, zdt);
-}
-
 static void courant_general(MixedState* m, DevStatus* st, cudaStream_t s)
 {
     dim3 grid((m->G.n[0] + 255) / 256, m->G.n[1], m->G.n[2]);
@@ -534,36 +540,48 @@ static void courant_general(MixedState* m, DevStatus* st, cudaStream_t s)
     }
 }
 
-void mixed_load_aos(MixedState* m, const double* aos, DevStatus* st, cudaStream_t s)
+void mixed_load_begin(MixedState* m, cudaStream_t s)
 {
-    const long long n = m->G.sP;
-    const int r = host_rot(m);
     cudaMemcpyAsync(m->drot, &m->rot, sizeof(int), cudaMemcpyHostToDevice, s);
-    const unsigned nb = (unsigned) ((n + 255) / 256);
-    switch (m->cfg.law) {
-        case MARA_LAW_HYDRO: load_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
-        case MARA_LAW_MHD: load_kernel<LAW_MHD><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
-        default: load_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(aos, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st); break;
-    }
-    // Courant step of the loaded state, published by mixed_enqueue_courant
     k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
-    if (m->fused) {
-        dim3 grid((m->G.n[0] + 255) / 256, m->G.n[1], 1);
-        courant_u_kernel<<<grid, 256, 0, s>>>(m->dgrid, m->drot, m->dcfl);
-    } else {
-        courant_general(m, st, s);
+}
+
+void mixed_load_aos_range(MixedState* m, const double* aos, long long c0, long long c1, DevStatus* st, cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    const int r = host_rot(m);
+    const unsigned nb = (unsigned) ((c1 - c0 + 255) / 256);
+    switch (m->cfg.law) {
+        case MARA_LAW_HYDRO:
+            // the fused form reduces the first Courant step here
+            load_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st,
+                                                      m->fused ? m->dcfl : nullptr);
+            break;
+        case MARA_LAW_MHD:
+            load_kernel<LAW_MHD><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st, nullptr);
+            break;
+        default:
+            load_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st, nullptr);
+            break;
     }
 }
 
-void mixed_store_aos(MixedState* m, double* aos, cudaStream_t s)
+void mixed_load_finish(MixedState* m, DevStatus* st, cudaStream_t s)
 {
-    const long long n = m->G.sP;
-    const unsigned nb = (unsigned) ((n + 255) / 256);
+    // Courant step of the loaded state (the general form reads the FP32
+    // primitives), published by mixed_enqueue_courant
+    if (!m->fused) courant_general(m, st, s);
+}
+
+void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    const unsigned nb = (unsigned) ((c1 - c0 + 255) / 256);
     const int r = host_rot(m);
     switch (m->cfg.law) {
-        case MARA_LAW_HYDRO: store_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
-        case MARA_LAW_MHD: store_kernel<LAW_MHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
-        default: store_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, m->GF, m->pp); break;
+        case MARA_LAW_HYDRO: store_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
+        case MARA_LAW_MHD: store_kernel<LAW_MHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
+        default: store_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
     }
 }
 

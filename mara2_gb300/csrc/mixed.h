@@ -13,8 +13,11 @@ struct MixedState;
 
 int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cudaStream_t s, int64_t* bytes);
 void mixed_destroy(MixedState* m);
-void mixed_load_aos(MixedState* m, const double* aos, DevStatus* st, cudaStream_t s);
-void mixed_store_aos(MixedState* m, double* aos, cudaStream_t s);
+// upload: begin, then the AoS cells [c0, c1) as their copies land, then finish
+void mixed_load_begin(MixedState* m, cudaStream_t s);
+void mixed_load_aos_range(MixedState* m, const double* aos, long long c0, long long c1, DevStatus* st, cudaStream_t s);
+void mixed_load_finish(MixedState* m, DevStatus* st, cudaStream_t s);
+void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s);
 void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t* timed);
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);
 int mixed_launches_per_step(const MixedState* m);
