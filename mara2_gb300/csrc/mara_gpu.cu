@@ -462,9 +462,13 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
     (void) t0;
     if (!h) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
-    launch_set_dt(h->st, dt, h->stream);
-    h->launches++;
-    enqueue_step(h);
+    if (h->mixed && mixed_enqueue_advance(h->mixed, dt, h->st, h->stream)) {
+        h->launches += mixed_launches_per_step(h->mixed);
+    } else {
+        launch_set_dt(h->st, dt, h->stream);
+        h->launches++;
+        enqueue_step(h);
+    }
     h->steps++;
     return cuda_status(cudaGetLastError());
 }
@@ -488,6 +492,20 @@ int mara_gpu_courant(MaraGpuHandle* h, double* dt)
     return rc;
 }
 
+// one driver-loop step: Courant step, dt, the RK stages, the clock
+static void enqueue_run_step(MaraGpuHandle* h, double cfl, double t_final)
+{
+    if (h->mixed && mixed_enqueue_run_step(h->mixed, cfl, t_final, h->st, h->stream)) {
+        h->launches += mixed_launches_per_step(h->mixed);
+        return;
+    }
+    enqueue_courant(h);
+    launch_dt_from_courant(h->st, cfl, t_final, h->stream);
+    enqueue_step(h);
+    launch_advance_time(h->st, h->stream);
+    h->launches += 2;
+}
+
 static int build_run_graph(MaraGpuHandle* h, int which, double cfl, double t_final)
 {
     cudaGraph_t g;
@@ -495,10 +513,7 @@ static int build_run_graph(MaraGpuHandle* h, int which, double cfl, double t_fin
     h->timing = 0;
     const int64_t launches = h->launches;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_courant(h);
-    launch_dt_from_courant(h->st, cfl, t_final, h->stream);
-    enqueue_step(h);
-    launch_advance_time(h->st, h->stream);
+    enqueue_run_step(h, cfl, t_final);
     CK(cudaStreamEndCapture(h->stream, &g));
     h->timing = timing;
     h->launches = launches;
@@ -510,6 +525,7 @@ static int build_run_graph(MaraGpuHandle* h, int which, double cfl, double t_fin
 
 static int launches_per_run_step(MaraGpuHandle* h)
 {
+    if (h->mixed && mixed_fused(h->mixed)) return mixed_launches_per_step(h->mixed);
     int n = 2 /* courant init + courant */ + 2 /* dt, time */;
     if (h->mixed) return n + mixed_launches_per_step(h->mixed);
     for (int a = 0; a < 3; ++a) if (h->G.n[a] > 1) n += h->cfg.rk_order;
@@ -542,11 +558,7 @@ static int enqueue_run(MaraGpuHandle* h, int max_steps, double cfl, double t_fin
             else h->cur = (h->cur + h->cfg.rk_order) & 1;
             h->launches += launches_per_run_step(h);
         } else {
-            enqueue_courant(h);
-            launch_dt_from_courant(h->st, cfl, t_final, h->stream);
-            enqueue_step(h);
-            launch_advance_time(h->st, h->stream);
-            h->launches += 2;
+            enqueue_run_step(h, cfl, t_final);
         }
         h->steps++;
     }

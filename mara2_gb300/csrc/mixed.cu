@@ -385,6 +385,36 @@ __global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long l
 __global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
 __global__ void k_rot_flip(int* rot) { *rot ^= 1; }
 
+// Start of one driver-loop step of the fused path, in one thread: the Courant
+// step that the previous step's last stage (or the load) reduced becomes the
+// handle's, dt = min(cfl x courant, t_final - t) (src/Problems.cpp:181-186),
+// the reduction slot is reset for this step's last stage, and the clock
+// advances (the fused hydro stages record no inversion failures, so the step
+// cannot fail after this point).
+__global__ void k_fused_run_begin(unsigned long long* bits, DevStatus* st, double cfl, double t_final)
+{
+    if (st->done) return;
+    st->dt_bits = *bits;
+    double dt = cfl * __longlong_as_double((long long) st->dt_bits);
+    if (t_final >= 0.0) {
+        if (!(st->t < t_final)) { st->done = 1; return; }
+        const double dt2 = t_final - st->t;
+        dt = dt < dt2 ? dt : dt2;
+    }
+    st->dt = dt;
+    *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
+    if (st->code) return;
+    st->t += dt;
+    st->steps += 1;
+}
+
+// Start of one advance with a given dt on the fused path.
+__global__ void k_fused_advance_begin(unsigned long long* bits, DevStatus* st, double dt)
+{
+    st->dt = dt;
+    *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
+}
+
 // ---------------------------------------------------------------------------
 struct MixedState {
     MaraGpuConfig cfg;
@@ -679,12 +709,12 @@ static void tile_dispatch(MixedState* m, const double* dt, DevStatus* st, cudaSt
     }
 }
 
+// the stages of one step; the Courant reduction slot has been reset
 static void fused_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s)
 {
     const int order = m->cfg.rk_order;
     for (int rk = 0; rk < order; ++rk) {
         const int last = rk == order - 1;
-        if (last) k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
         const float b = B_TAB[order - 1][rk];
         timed(m, s, [&] {
             if (m->G.n[1] > 1) tile_dispatch<2>(m, dt, st, s, rk, b, last);
@@ -696,14 +726,37 @@ static void fused_step(MixedState* m, const double* dt, DevStatus* st, cudaStrea
 
 void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t*)
 {
-    if (m->fused) fused_step(m, dt, st, s);
-    else general_step(m, dt, st, s);
+    if (m->fused) {
+        k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
+        fused_step(m, dt, st, s);
+    } else {
+        general_step(m, dt, st, s);
+    }
     if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1;
+}
+
+bool mixed_enqueue_run_step(MixedState* m, double cfl, double t_final, DevStatus* st, cudaStream_t s)
+{
+    if (!m->fused) return false;
+    k_fused_run_begin<<<1, 1, 0, s>>>(m->dcfl, st, cfl, t_final);
+    fused_step(m, &st->dt, st, s);
+    if (m->cfg.rk_order == 1) m->rot ^= 1;
+    return true;
+}
+
+bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t s)
+{
+    if (!m->fused) return false;
+    k_fused_advance_begin<<<1, 1, 0, s>>>(m->dcfl, st, dt);
+    fused_step(m, &st->dt, st, s);
+    if (m->cfg.rk_order == 1) m->rot ^= 1;
+    return true;
 }
 
 int mixed_launches_per_step(const MixedState* m)
 {
-    if (m->fused) return m->cfg.rk_order + 1 + (m->cfg.rk_order == 1 ? 1 : 0);
+    // fused: the step-begin kernel, one launch per stage, the RK1 rotation
+    if (m->fused) return 1 + m->cfg.rk_order + (m->cfg.rk_order == 1 ? 1 : 0);
     int axes = 0;
     for (int a = 0; a < 3; ++a) axes += m->G.n[a] > 1;
     return m->cfg.rk_order * (axes + 1) + 2;
@@ -711,6 +764,7 @@ int mixed_launches_per_step(const MixedState* m)
 
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s) { k_cfl_publish<<<1, 1, 0, s>>>(m->dcfl, st); }
 int mixed_parity(const MixedState* m) { return m->rot & 1; }
+bool mixed_fused(const MixedState* m) { return m->fused; }
 void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
 void mixed_advance_parity(MixedState* m) { if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1; }
 void mixed_set_timing(MixedState* m, int on) { m->timing = on; }

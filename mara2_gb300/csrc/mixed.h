@@ -20,7 +20,13 @@ void mixed_load_finish(MixedState* m, DevStatus* st, cudaStream_t s);
 void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s);
 void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t* timed);
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);
+// One whole driver-loop step (dt from the Courant step, stages, clock) or one
+// advance with a given dt, when the fused hydro kernels apply; false (nothing
+// enqueued) otherwise.
+bool mixed_enqueue_run_step(MixedState* m, double cfl, double t_final, DevStatus* st, cudaStream_t s);
+bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t s);
 int mixed_launches_per_step(const MixedState* m);
+bool mixed_fused(const MixedState* m);
 int mixed_parity(const MixedState* m);
 void mixed_set_parity(MixedState* m, int p);
 void mixed_advance_parity(MixedState* m);
