@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
         else if (stage == 1) { src = (s + 1) % 3; dst = last ? s : (s + 2) % 3; }
         else { src = (s + 2) % 3; dst = s; }
         const float* __restrict__ Uin = g.Uh[src];
+        const long long sU = g.sU;
+        const int n0 = g.n0, n1 = g.n1;
 
         // L2 prefetch of what the update phase reads per zone besides the
         // stage input's high word (already staged below): its low word and,
@@ -178,9 +180,9 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
             for (int l = threadIdx.x; l < lines; l += NT) {
                 const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
                 const int y = tr.y0 + r, x = tr.x0 + seg * 32;
-                if (y < g.n1 && x < g.n0) {
+                if (y < n1 && x < n0) {
                     const float* base = a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
-                    const float* ptr = base + q * g.sU + (long long) y * g.n0 + x;
+                    const float* ptr = base + q * sU + (long long) y * n0 + x;
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
                 }
             }
@@ -188,24 +190,43 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
 
         __syncthreads(); // the previous tile's shared data is consumed
         // 1. primitives of the tile and its halo: all loads first, then the
-        //    conversions, so each thread keeps NC x 5 loads in flight
+        //    conversions, so each thread keeps NC x 5 loads in flight.  A tile
+        //    whose halo lies inside the grid reads it as one rectangle; the
+        //    others take every halo zone from its boundary image.
         {
             constexpr int NC = (WX * WY + NT - 1) / NT;
             float Ur[NC][5];
             int fl[NC];
+            const bool inner = tr.x0 - G >= 0 && tr.x0 + TX + G <= n0 &&
+                               (DIM == 1 || (tr.y0 - G >= 0 && tr.y0 + TY + G <= n1));
+            if (inner) {
+                const float* base = Uin + (long long) (tr.y0 - (DIM == 2 ? G : 0)) * n0 + (tr.x0 - G);
 #pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                const int c = threadIdx.x + k * NT;
-                fl[k] = 0;
-                if (c < WX * WY) {
-                    const int lx = c % WX, ly = c / WX;
-                    int flipx = 0, flipy = 0;
-                    const int x = bc_image(tr.x0 + lx - G, g.n0, g.bc, flipx);
-                    const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, g.n1, g.bc, flipy) : 0;
-                    const long long o = (long long) y * g.n0 + x;
+                for (int k = 0; k < NC; ++k) {
+                    const int c = threadIdx.x + k * NT;
+                    fl[k] = 0;
+                    if (c < WX * WY) {
+                        const int lx = c % WX, ly = c / WX;
+                        const float* p = base + (long long) ly * n0 + lx;
 #pragma unroll
-                    for (int q = 0; q < 5; ++q) Ur[k][q] = Uin[q * g.sU + o];
-                    fl[k] = flipx | (flipy << 1);
+                        for (int q = 0; q < 5; ++q) Ur[k][q] = p[q * sU];
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    const int c = threadIdx.x + k * NT;
+                    fl[k] = 0;
+                    if (c < WX * WY) {
+                        const int lx = c % WX, ly = c / WX;
+                        int flipx = 0, flipy = 0;
+                        const int x = bc_image(tr.x0 + lx - G, n0, g.bc, flipx);
+                        const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, n1, g.bc, flipy) : 0;
+                        const long long o = (long long) y * n0 + x;
+#pragma unroll
+                        for (int q = 0; q < 5; ++q) Ur[k][q] = Uin[q * sU + o];
+                        fl[k] = flipx | (flipy << 1);
+                    }
                 }
             }
 #pragma unroll
@@ -224,6 +245,7 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
         }
         __syncthreads();
 
+        const float theta = g.plm_theta, gamma = g.gamma;
         // 2. x faces and y faces in one balanced loop (face fx sits left of
         //    tile zone fx, face fy below tile row fy)
         for (int f = threadIdx.x; f < FXN + (DIM == 2 ? FYN : 0); f += NT) {
@@ -236,10 +258,10 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
                     float v[2 * G];
 #pragma unroll
                     for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][ry][fx + m];
-                    recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
+                    recon_pair<RECON>(v, theta, PL[q], PR[q]);
                 }
                 const float nx[3] = {1.f, 0.f, 0.f};
-                hydro_face_flux<RIEMANN>(g.gamma, PL, PR, nx, Fh);
+                hydro_face_flux<RIEMANN>(gamma, PL, PR, nx, Fh);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Fx[q][fy][fx] = Fh[q];
             } else if constexpr (DIM == 2) {
@@ -250,10 +272,10 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
                     float v[2 * G];
 #pragma unroll
                     for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][fy + m][fx + G];
-                    recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
+                    recon_pair<RECON>(v, theta, PL[q], PR[q]);
                 }
                 const float ny[3] = {0.f, 1.f, 0.f};
-                hydro_face_flux<RIEMANN>(g.gamma, PL, PR, ny, Fh);
+                hydro_face_flux<RIEMANN>(gamma, PL, PR, ny, Fh);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Fy[q][fy][fx] = Fh[q];
             }
@@ -263,21 +285,29 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
         // 3. divergence, RK combine, store
         const float dt = (float) dtg[tr.grid * dt_stride];
         float zdt = 3.0e38f;
+        // the rotation's three buffers are distinct arrays
+        const float* __restrict__ U0h = g.Uh[s];
+        const float* __restrict__ U0l = g.Ul[s];
+        const float* __restrict__ Uph = g.Uh[src];
+        const float* __restrict__ Upl = g.Ul[src];
+        float* __restrict__ Unh = g.Uh[dst];
+        float* __restrict__ Unl = g.Ul[dst];
+        const float idx = g.idx, idy = g.idy;
         for (int c = threadIdx.x; c < TX * TY; c += NT) {
             const int lx = c % TX, ly = c / TX;
             const int x = tr.x0 + lx, y = tr.y0 + ly;
-            if (x >= g.n0 || y >= g.n1) continue;
-            const long long o = (long long) y * g.n0 + x;
+            if (x >= n0 || y >= n1) continue;
+            const long long o = (long long) y * n0 + x;
             float Unew[5];
 #pragma unroll
             for (int q = 0; q < 5; ++q) {
-                float L = -(Fx[q][ly][lx + 1] - Fx[q][ly][lx]) * g.idx;
-                if constexpr (DIM == 2) L -= (Fy[q][ly + 1][lx] - Fy[q][ly][lx]) * g.idy;
-                const df U0 = {g.Uh[s][q * g.sU + o], g.Ul[s][q * g.sU + o]};
-                const df Up = {g.Uh[src][q * g.sU + o], g.Ul[src][q * g.sU + o]};
+                float L = -(Fx[q][ly][lx + 1] - Fx[q][ly][lx]) * idx;
+                if constexpr (DIM == 2) L -= (Fy[q][ly + 1][lx] - Fy[q][ly][lx]) * idy;
+                const df U0 = {U0h[q * sU + o], U0l[q * sU + o]};
+                const df Up = {Uph[q * sU + o], Upl[q * sU + o]};
                 const df Un = rk_combine(U0, Up, dt * L, b, omb);
-                g.Uh[dst][q * g.sU + o] = Un.hi;
-                g.Ul[dst][q * g.sU + o] = Un.lo;
+                Unh[q * sU + o] = Un.hi;
+                Unl[q * sU + o] = Un.lo;
                 Unew[q] = Un.hi;
             }
             if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));

@@ -462,6 +462,7 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
     (void) t0;
     if (!h) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    if (h->mixed) mixed_set_timing(h->mixed, h->timing);
     if (h->mixed && mixed_enqueue_advance(h->mixed, dt, h->st, h->stream)) {
         h->launches += mixed_launches_per_step(h->mixed);
     } else {
@@ -495,6 +496,7 @@ int mara_gpu_courant(MaraGpuHandle* h, double* dt)
 // one driver-loop step: Courant step, dt, the RK stages, the clock
 static void enqueue_run_step(MaraGpuHandle* h, double cfl, double t_final)
 {
+    if (h->mixed) mixed_set_timing(h->mixed, h->timing);
     if (h->mixed && mixed_enqueue_run_step(h->mixed, cfl, t_final, h->st, h->stream)) {
         h->launches += mixed_launches_per_step(h->mixed);
         return;

@@ -81,3 +81,20 @@ def test_mixed_courant_close(gpu_lib, port):
         g.upload(P.copy())
         dt = g.courant()
     assert abs(dt - dt_ref) / dt_ref < 1e-6
+
+
+@pytest.mark.gpu
+def test_kernel_timing_counts_stage_launches(gpu_lib):
+    """Per-launch kernel timing (the benchmark's roofline source) sees every
+    stage launch of the fused path, through run() and advance()."""
+    s, P = W.kelvin_helmholtz(64)
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        g.set_kernel_timing(True)
+        g.run(3)
+        dt = g.courant() * s.cfl
+        g.advance(dt)
+        ms, n = g.kernel_times()
+        g.set_kernel_timing(False)
+    assert n[0] == 4 * s.rk_order, n
+    assert ms[0] > 0.0
