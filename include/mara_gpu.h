@@ -154,6 +154,31 @@ int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches
  * (the reference's default is 1).  MHD and RMHD only. */
 int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs);
 
+/* Number of volume-integrated diagnostics the law lists
+ * (ConservationLaw::getDiagnosticNames, ConservationLaws.cpp:332-341,
+ * 576-601, 924-945): 5 for hydro (mass, momentum1-3, total_energy), 17 for
+ * MHD and RMHD (those, magnetic_flux1-3, kinetic_energy, internal_energy,
+ * magnetic_energy, sound_speed, alfven_speed, sonic_mach_number,
+ * alfven_mach_number, specific_entropy, cross_helicity). */
+int mara_gpu_num_diagnostics(const MaraGpuHandle* h);
+
+/* FieldOperator::volumeIntegratedDiagnostics (FieldOperator.cpp:171-205) of
+ * the resident state over the interior zones: per zone makeDiagnostics of
+ * fromPrimitive(P), times the cell volume, summed (totals equal the
+ * reference's to rounding; the summation order differs).  On the mixed path
+ * P is the FP64 state a download returns.  D holds mara_gpu_num_diagnostics
+ * values; *count (if not NULL) receives that number.  A zone whose state the
+ * law rejects makes the call return its status code. */
+int mara_gpu_volume_diagnostics(MaraGpuHandle* h, double* D, int* count);
+
+/* The cell diagnostic fields a checkpoint carries (the reference's checkpoint
+ * task, src/Problems/MagneticBraiding.cpp:176-189):
+ * CellCenteredFieldCT::monopole and ::current at cell centres
+ * (CellCenteredFieldCT.cpp:159-257) of the resident magnetic field at every
+ * cell of the array with guards, as FP64 AoS (ni+2g, nj+2g, nk+2g, 4) =
+ * [monopole, current1, current2, current3].  MHD and RMHD only. */
+int mara_gpu_field_diagnostics(MaraGpuHandle* h, double mesh_spacing, double* out_aos);
+
 /* Device bytes the handle holds. */
 int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
 

@@ -69,6 +69,9 @@ SIGNATURES = {
     "mara_gpu_kernel_times": (C.c_int, [_H, _D, C.POINTER(C.c_int64)]),
     "mara_gpu_device_bytes": (C.c_int64, [_H]),
     "mara_gpu_monopole": (C.c_int, [_H, C.c_double, _D]),
+    "mara_gpu_num_diagnostics": (C.c_int, [_H]),
+    "mara_gpu_volume_diagnostics": (C.c_int, [_H, C.c_void_p, C.POINTER(C.c_int)]),
+    "mara_gpu_field_diagnostics": (C.c_int, [_H, C.c_double, C.c_void_p]),
     "mara_gpu_status_string": (C.c_char_p, [C.c_int]),
     "mara_gpu_advance_noalloc": (C.c_int, [C.POINTER(MaraGpuConfig), C.c_void_p, C.c_void_p, C.c_double,
                                            C.c_void_p]),

@@ -22,6 +22,7 @@
 #include <stdexcept>
 #include <string>
 #include <typeinfo>
+#include <vector>
 
 #include "BoundaryConditions.hpp"
 #include "CartesianMeshGeometry.hpp"
@@ -91,6 +92,31 @@ public:
         double dt = 0.0;
         raise (mara_gpu_courant (handle, &dt));
         return dt;
+    }
+
+    /** FieldOperator::volumeIntegratedDiagnostics of solution.P (interior)
+     *  with the cell volumes, on the GPU; the order of
+     *  ConservationLaw::getDiagnosticNames. */
+    std::vector<double> volumeIntegratedDiagnostics (MeshData& solution) const
+    {
+        ensure (solution);
+        raise (mara_gpu_upload (handle, solution.P.data()));
+        auto D = std::vector<double> (mara_gpu_num_diagnostics (handle));
+        raise (mara_gpu_volume_diagnostics (handle, D.data(), nullptr));
+        return D;
+    }
+
+    /** CellCenteredFieldCT::monopole and ::current (MeshLocation::cell) of
+     *  the cell magnetic field of solution.P including guards, as the
+     *  drivers' checkpoint task stores them: shape (ni+2g, nj+2g, nk+2g, 4),
+     *  components [monopole, current1, current2, current3]. */
+    Cow::Array fieldDiagnostics (MeshData& solution, double meshSpacing) const
+    {
+        ensure (solution);
+        raise (mara_gpu_upload (handle, solution.P.data()));
+        auto D = Cow::Array (solution.P.size (0), solution.P.size (1), solution.P.size (2), 4, 1);
+        raise (mara_gpu_field_diagnostics (handle, meshSpacing, D.data()));
+        return D;
     }
 
 private:

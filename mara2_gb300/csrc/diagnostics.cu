@@ -1,50 +1,36 @@
-// diagnostics.cu -- device diagnostics of the resident state.
+// diagnostics.cu -- device diagnostics of the resident state (the kernels are
+// in diagnostics.cuh).
 //
-// monopole: CellCenteredFieldCT::monopole with MeshLocation::cell
-// (CellCenteredFieldCT.cpp:159-223): div B at the mesh vertices from the 8
-// cells around each vertex, then averaged onto cells; reduced here to the
-// largest |div B| over the interior zones (the figure the MHD workload
-// reports).  Reads the cell-centred field from the primitive array with
-// guards (FP64 on the plain path, FP32 on the mixed path).
+// monopole max: CellCenteredFieldCT::monopole with MeshLocation::cell
+// (CellCenteredFieldCT.cpp:159-223) reduced to the largest |div B| over the
+// interior zones (the figure the MHD workload reports).  Reads the
+// cell-centred field from the primitive array with guards (FP64 on the plain
+// path, FP32 on the mixed path).
 #include <cuda_runtime.h>
 
+#include "diagnostics.cuh"
 #include "internal.h"
 
 namespace mara {
 
 template <typename T>
-__device__ __forceinline__ double vertex_monopole(const T* __restrict__ P, const GridDesc& G, int a, int b, int c,
-                                                  double h)
+static CellB<T> cell_b(const void* P, const GridDesc& G)
 {
-    // vertex (a, b, c) sits at the low corner of cell (a, b, c); the
-    // reference writes M(i+1, j+1, k+1) from cells (i..i+r, j..j+s, k..k+t)
-    const int r = G.N[0] > 1, s = G.N[1] > 1, t = G.N[2] > 1;
-    const int i = a - 1, j = b - 1, k = c - 1;
-    if (i < 0 || j < 0 || k < 0 || i >= G.N[0] - r || j >= G.N[1] - s || k >= G.N[2] - t) return 0.0;
-    auto B = [&](int ii, int jj, int kk, int comp) -> double {
-        return (double) P[(5 + comp) * G.sP + ((long long) kk * G.N[1] + jj) * G.N[0] + ii];
-    };
-    const double Bx0 = B(i, j, k, 0) + B(i, j, k + t, 0) + B(i, j + s, k, 0) + B(i, j + s, k + t, 0);
-    const double Bx1 = B(i + r, j, k, 0) + B(i + r, j, k + t, 0) + B(i + r, j + s, k, 0) + B(i + r, j + s, k + t, 0);
-    const double By0 = B(i, j, k, 1) + B(i + r, j, k, 1) + B(i, j, k + t, 1) + B(i + r, j, k + t, 1);
-    const double By1 = B(i, j + s, k, 1) + B(i + r, j + s, k, 1) + B(i, j + s, k + t, 1) + B(i + r, j + s, k + t, 1);
-    const double Bz0 = B(i, j, k, 2) + B(i, j + s, k, 2) + B(i + r, j, k, 2) + B(i + r, j + s, k, 2);
-    const double Bz1 = B(i, j, k + t, 2) + B(i, j + s, k + t, 2) + B(i + r, j, k + t, 2) + B(i + r, j + s, k + t, 2);
-    return 0.25 * ((Bx1 - Bx0) + (By1 - By0) + (Bz1 - Bz0)) / h;
+    return CellB<T>{(const T*) P, G.sP, G.N[0], G.N[1], G.N[2]};
 }
 
 template <typename T>
-__global__ void k_monopole_max(const T* __restrict__ P, GridDesc G, double h, unsigned long long* out)
+__global__ void k_monopole_max(CellB<T> B, GridDesc G, double h, unsigned long long* out)
 {
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
     double m = 0.0;
     if (ii < G.n[0]) {
         // cell-centred monopole of an interior zone (full indices)
         const int i = ii + G.g[0], j = blockIdx.y + G.g[1], k = blockIdx.z + G.g[2];
-        const double M000 = vertex_monopole(P, G, i, j, k, h);
-        const double Mi = M000 + vertex_monopole(P, G, i + 1, j, k, h);
-        const double Mj = M000 + vertex_monopole(P, G, i, j + 1, k, h);
-        const double Mk = M000 + vertex_monopole(P, G, i, j, k + 1, h);
+        const double M000 = vertex_monopole_at(B, i, j, k, h);
+        const double Mi = M000 + vertex_monopole_at(B, i + 1, j, k, h);
+        const double Mj = M000 + vertex_monopole_at(B, i, j + 1, k, h);
+        const double Mk = M000 + vertex_monopole_at(B, i, j, k + 1, h);
         m = fabs(1. / 6 * (Mi + Mj + Mk));
     }
     unsigned long long b = (unsigned long long) __double_as_longlong(m);
@@ -61,8 +47,60 @@ void launch_monopole_max(const void* P, bool fp32, const GridDesc& G, double h, 
                          cudaStream_t s)
 {
     dim3 grid((G.n[0] + 255) / 256, G.n[1], G.n[2]);
-    if (fp32) k_monopole_max<float><<<grid, 256, 0, s>>>((const float*) P, G, h, out);
-    else k_monopole_max<double><<<grid, 256, 0, s>>>((const double*) P, G, h, out);
+    if (fp32) k_monopole_max<float><<<grid, 256, 0, s>>>(cell_b<float>(P, G), G, h, out);
+    else k_monopole_max<double><<<grid, 256, 0, s>>>(cell_b<double>(P, G), G, h, out);
+}
+
+void launch_field_diag(const void* P, bool fp32, const GridDesc& G, double h, double* out, cudaStream_t s)
+{
+    const long long total = (long long) G.N[0] * G.N[1] * G.N[2];
+    const unsigned nb = (unsigned) ((total + 255) / 256);
+    if (fp32) k_field_diag<float><<<nb, 256, 0, s>>>(cell_b<float>(P, G), h, out);
+    else k_field_diag<double><<<nb, 256, 0, s>>>(cell_b<double>(P, G), h, out);
+}
+
+// interior zone (i, j, k) of the plain path's FP64 primitives with guards
+template <int NQ>
+struct PlainSrc {
+    const double* P;
+    long long sP;
+    int N0, N1, g0, g1, g2;
+    __device__ __forceinline__ int load(int i, int j, int k, double* out) const
+    {
+        const long long o = ((long long) (k + g2) * N1 + (j + g1)) * N0 + (i + g0);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) out[q] = P[q * sP + o];
+        return ST_OK;
+    }
+};
+
+template <int LAW>
+static void volume_diag_plain(const double* P, const GridDesc& G, const PhysParams& pp, double* partial, int* err,
+                              double* out, cudaStream_t s)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    const PlainSrc<NQ> src{P, G.sP, G.N[0], G.N[1], G.g[0], G.g[1], G.g[2]};
+    const long long zones = (long long) G.n[0] * G.n[1] * G.n[2];
+    const long long want = (zones + 255) / 256;
+    const int nb = (int) (want < DIAG_BLOCKS ? want : DIAG_BLOCKS);
+    k_volume_diag<LAW><<<nb, 256, 0, s>>>(src, pp, G.n[0], G.n[1], zones, G.dV, partial, err);
+    k_diag_final<<<1, 32, 0, s>>>(partial, nb, DiagInfo<LAW>::ND, out);
+}
+
+void launch_volume_diag_plain(int law, const double* P, const GridDesc& G, const PhysParamsH& ph, double* partial,
+                              int* err, double* out, cudaStream_t s)
+{
+    PhysParams pp;
+    pp.gamma = ph.gamma;
+    pp.plm_theta = ph.plm_theta;
+    pp.shenzha_A = ph.shenzha_A;
+    pp.pressure_floor = ph.pressure_floor;
+    pp.weno_is = ph.weno_is;
+    switch (law) {
+        case LAW_HYDRO: volume_diag_plain<LAW_HYDRO>(P, G, pp, partial, err, out, s); break;
+        case LAW_MHD: volume_diag_plain<LAW_MHD>(P, G, pp, partial, err, out, s); break;
+        default: volume_diag_plain<LAW_RMHD>(P, G, pp, partial, err, out, s); break;
+    }
 }
 
 } // namespace mara

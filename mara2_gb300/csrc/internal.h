@@ -60,6 +60,13 @@ void plain_courant(int law, const GridDesc& G, const PhysParamsH& pp, const doub
 // ---- diagnostics (diagnostics.cu) ----------------------------------------------
 void launch_monopole_max(const void* P, bool fp32, const GridDesc& G, double h, unsigned long long* out,
                          cudaStream_t s);
+// monopole and current at every cell of the array with guards, FP64 AoS
+// (N0, N1, N2, 4)
+void launch_field_diag(const void* P, bool fp32, const GridDesc& G, double h, double* out, cudaStream_t s);
+// volume-integrated diagnostics of the plain path's primitives: per-block
+// partial sums (DIAG_BLOCKS x 17 doubles), the first error code, the totals
+void launch_volume_diag_plain(int law, const double* P, const GridDesc& G, const PhysParamsH& pp, double* partial,
+                              int* err, double* out, cudaStream_t s);
 
 // ---- shared helpers (mara_gpu.cu) --------------------------------------------
 void launch_courant_init(DevStatus* st, cudaStream_t s);

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/mara_gpu.h"
+#include "diagnostics.cuh"
 #include "internal.h"
 #include "mixed.h"
 
@@ -153,6 +154,7 @@ struct MaraGpuHandle {
     int64_t timed_launches[3] = {0, 0, 0};
     int last_status = 0;
     MaraGpuStats last_stats;
+    double* diag = nullptr;              // diagnostics scratch: partial sums, totals, error word
 };
 
 static int cuda_status(cudaError_t e)
@@ -389,6 +391,7 @@ int mara_gpu_destroy(MaraGpuHandle* h)
     for (int a = 0; a < 3; ++a) cudaFree(h->F[a]);
     cudaFree(h->stage_aos);
     cudaFree(h->st);
+    cudaFree(h->diag);
     if (h->mixed) mixed_destroy(h->mixed);
     if (h->st_host) cudaFreeHost(h->st_host);
     for (int e = 0; e < 17; ++e) if (h->ev[e]) cudaEventDestroy(h->ev[e]);
@@ -673,6 +676,59 @@ int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs)
     CK(cudaMemcpyAsync(&bits, out, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     *max_abs = __builtin_bit_cast(double, bits);
+    return MARA_OK;
+}
+
+int mara_gpu_num_diagnostics(const MaraGpuHandle* h)
+{
+    if (!h) return 0;
+    return h->cfg.law == MARA_LAW_HYDRO ? 5 : 17;
+}
+
+int mara_gpu_volume_diagnostics(MaraGpuHandle* h, double* D, int* count)
+{
+    if (!h || !D) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    const size_t nd = DIAG_MAX;
+    const size_t doubles = (size_t) DIAG_BLOCKS * nd + nd + 1;  // partials, totals, error word
+    if (!h->diag) {
+        if (alloc(h, (void**) &h->diag, doubles * sizeof(double))) return MARA_ERR_CUDA;
+    }
+    double* partial = h->diag;
+    double* out = h->diag + (size_t) DIAG_BLOCKS * nd;
+    int* err = (int*) (out + nd);
+    CK(cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+    if (h->mixed) mixed_volume_diagnostics(h->mixed, partial, err, out, h->stream);
+    else launch_volume_diag_plain(h->cfg.law, h->P[h->cur], h->G, h->pp, partial, err, out, h->stream);
+    h->launches += 3;
+    const int n = mara_gpu_num_diagnostics(h);
+    double host[DIAG_MAX + 1];
+    CK(cudaMemcpyAsync(host, out, sizeof(double) * (nd + 1), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int e = 0;
+    std::memcpy(&e, &host[nd], sizeof(int));
+    if (e) return e;
+    for (int q = 0; q < n; ++q) D[q] = host[q];
+    if (count) *count = n;
+    return MARA_OK;
+}
+
+int mara_gpu_field_diagnostics(MaraGpuHandle* h, double mesh_spacing, double* out_aos)
+{
+    if (!h || !out_aos || !(mesh_spacing > 0.0)) return MARA_ERR_ARGUMENT;
+    if (h->cfg.law == MARA_LAW_HYDRO) return MARA_ERR_CONFIG;
+    CK(cudaSetDevice(h->cfg.device));
+    const void* P = h->mixed ? (const void*) mixed_primitives(h->mixed) : (const void*) h->P[h->cur];
+    if (!P) return MARA_ERR_CONFIG;
+    const size_t bytes = (size_t) h->G.N[0] * h->G.N[1] * h->G.N[2] * 4 * sizeof(double);
+    double* d = nullptr;
+    CK(cudaMallocAsync((void**) &d, bytes, h->stream));
+    launch_field_diag(P, h->mixed != nullptr, h->G, mesh_spacing, d, h->stream);
+    h->launches++;
+    const cudaError_t e = cudaMemcpyAsync(out_aos, d, bytes, cudaMemcpyDeviceToHost, h->stream);
+    cudaFreeAsync(d, h->stream);
+    CK(e);
+    CK(cudaStreamSynchronize(h->stream));
     return MARA_OK;
 }
 

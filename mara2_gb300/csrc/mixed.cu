@@ -14,6 +14,7 @@
 #include <cstring>
 #include <vector>
 
+#include "diagnostics.cuh"
 #include "hydro_tile.cuh"
 #include "mixed.h"
 #include "physics_fp32.cuh"
@@ -612,6 +613,56 @@ void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c
         case MARA_LAW_HYDRO: store_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
         case MARA_LAW_MHD: store_kernel<LAW_MHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
         default: store_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
+    }
+}
+
+// ---- diagnostics ---------------------------------------------------------------
+// interior zone (i, j, k) of the FP32-pair state, converted to FP64
+// primitives exactly as a download converts it
+template <int LAW>
+struct MixedSrc {
+    const float* Uh;
+    const float* Ul;
+    long long sU;
+    int n0, n1;
+    double gm1;
+    PhysParams pp;
+    __device__ __forceinline__ int load(int i, int j, int k, double* P) const
+    {
+        constexpr int NQ = LawInfo<LAW>::NQ;
+        const long long u = ((long long) k * n1 + j) * n0 + i;
+        double U[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) U[q] = (double) Uh[q * sU + u] + (double) Ul[q * sU + u];
+        if constexpr (LAW == LAW_HYDRO) {
+            hydro_u2p_d(U, gm1, P);
+            return ST_OK;
+        } else {
+            int code = 0;
+            const int e = law_cons<LAW>(pp, U, P, &code);
+            return e == ST_OK ? ST_OK : (code != 0 ? code : e);
+        }
+    }
+};
+
+template <int LAW>
+static void volume_diag_mixed(MixedState* m, double* partial, int* err, double* out, cudaStream_t s)
+{
+    const int r = host_rot(m);
+    const MixedSrc<LAW> src{m->Uh[r], m->Ul[r], m->GF.sU, m->G.n[0], m->G.n[1], m->GF.gm1_d, m->pp};
+    const long long zones = (long long) m->G.n[0] * m->G.n[1] * m->G.n[2];
+    const long long want = (zones + 255) / 256;
+    const int nb = (int) (want < DIAG_BLOCKS ? want : DIAG_BLOCKS);
+    k_volume_diag<LAW><<<nb, 256, 0, s>>>(src, m->pp, m->G.n[0], m->G.n[1], zones, m->G.dV, partial, err);
+    k_diag_final<<<1, 32, 0, s>>>(partial, nb, DiagInfo<LAW>::ND, out);
+}
+
+void mixed_volume_diagnostics(MixedState* m, double* partial, int* err, double* out, cudaStream_t s)
+{
+    switch (m->cfg.law) {
+        case MARA_LAW_HYDRO: volume_diag_mixed<LAW_HYDRO>(m, partial, err, out, s); break;
+        case MARA_LAW_MHD: volume_diag_mixed<LAW_MHD>(m, partial, err, out, s); break;
+        default: volume_diag_mixed<LAW_RMHD>(m, partial, err, out, s); break;
     }
 }
 

@@ -34,5 +34,8 @@ void mixed_set_timing(MixedState* m, int on);
 void mixed_kernel_times(MixedState* m, double ms[3], int64_t launches[3]);
 // FP32 primitives with guards of the general form (nullptr for the fused form)
 const float* mixed_primitives(const MixedState* m);
+// volume-integrated diagnostics of the state a download would return
+// (partial: DIAG_BLOCKS x 17 doubles; err: first error code; out: totals)
+void mixed_volume_diagnostics(MixedState* m, double* partial, int* err, double* out, cudaStream_t s);
 
 } // namespace mara

@@ -14,6 +14,17 @@ from . import _native as N
 from .scheme import Scheme
 
 
+def diagnostic_names(law: str) -> list:
+    """ConservationLaw::getDiagnosticNames (src/ConservationLaws.cpp:332-341,
+    576-601, 924-945)."""
+    base = ["mass", "momentum1", "momentum2", "momentum3", "total_energy"]
+    if law == "hydro":
+        return base
+    return base + ["magnetic_flux1", "magnetic_flux2", "magnetic_flux3", "kinetic_energy", "internal_energy",
+                   "magnetic_energy", "sound_speed", "alfven_speed", "sonic_mach_number", "alfven_mach_number",
+                   "specific_entropy", "cross_helicity"]
+
+
 class Solver:
     def __init__(self, scheme: Scheme, precision: str = "fp64", device: int = 0):
         self.scheme = scheme
@@ -127,6 +138,24 @@ class Solver:
 
     def set_kernel_timing(self, on: bool) -> None:
         self.lib.mara_gpu_set_kernel_timing(self.h, int(on))
+
+    def volume_diagnostics(self) -> dict:
+        """FieldOperator::volumeIntegratedDiagnostics of the resident state,
+        by the names ConservationLaw::getDiagnosticNames gives them."""
+        n = self.lib.mara_gpu_num_diagnostics(self.h)
+        D = np.zeros(n)
+        cnt = C.c_int(0)
+        N.check(self.lib.mara_gpu_volume_diagnostics(self.h, D.ctypes.data, C.byref(cnt)),
+                "mara_gpu_volume_diagnostics")
+        return dict(zip(diagnostic_names(self.scheme.law), D.tolist()))
+
+    def field_diagnostics(self, mesh_spacing: float = 1.0) -> np.ndarray:
+        """[monopole, current1, current2, current3] at every cell of the array
+        with guards, shape full_shape[:3] + (4,) (MHD and RMHD)."""
+        out = np.zeros(tuple(self.scheme.full_shape[:3]) + (4,))
+        N.check(self.lib.mara_gpu_field_diagnostics(self.h, mesh_spacing, out.ctypes.data),
+                "mara_gpu_field_diagnostics")
+        return out
 
     def kernel_times(self):
         ms = (C.c_double * 3)()

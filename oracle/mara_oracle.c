@@ -1336,3 +1336,127 @@ void mo_monopole_cell(const double* B, int n0, int n1, int n2, double h, double*
 #undef BI
 #undef MI
 }
+
+/* ------------------------------------------------------------------------ */
+/* ConservationLaw::makeDiagnostics of one primitive state                   */
+/* (NewtonianHydro ConservationLaws.cpp:321-330, NewtonianMHD :536-574 with  */
+/* no auxiliary fields, RelativisticMHD :874-922); the state comes from      */
+/* fromPrimitive with the default Request (area element x-hat,               */
+/* ConservationLaws.cpp:146-157)                                             */
+/* ------------------------------------------------------------------------ */
+int mo_num_diagnostics(const mo_config* c)
+{
+    switch (c->law) {
+        case MO_LAW_HYDRO: return 5;
+        case MO_LAW_MHD: return 17;
+        case MO_LAW_RMHD: return 17;
+        default: return 0;
+    }
+}
+
+static int make_diagnostics(const mo_config* c, const double* P, double* D)
+{
+    static const double xhat[3] = {1.0, 0.0, 0.0};
+    mstate S;
+    const int err = from_prim(c, P, xhat, &S);
+    if (err) return err;
+    if (c->law == MO_LAW_HYDRO) {
+        for (int q = 0; q < 5; ++q) D[q] = S.U[q];
+        return MO_OK;
+    }
+    const double gm = c->gamma;
+    const double vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
+    const double BB = P[5] * P[5] + P[6] * P[6] + P[7] * P[7];
+    const double Bv = P[5] * P[1] + P[6] * P[2] + P[7] * P[3];
+    const double cs = sqrt(gm * P[4] / P[0]);
+    const double ca = sqrt(BB / P[0]);
+    const double s0 = P[4] / pow(P[0], gm);
+    const double Ms = sqrt(vv) / cs;
+    const double Ma = sqrt(vv) / ca;
+    for (int q = 0; q < 8; ++q) D[q] = S.U[q];
+    if (c->law == MO_LAW_MHD) {
+        D[8] = 0.5 * vv * P[0];     /* kinetic energy  */
+        D[9] = P[4] / (gm - 1.0);   /* internal energy */
+        D[10] = 0.5 * BB;           /* magnetic energy */
+    } else {
+        const double v1 = P[1], v2 = P[2], v3 = P[3];
+        const double B1 = P[5], B2 = P[6], B3 = P[7];
+        const double E1 = -(v2 * B3 - v3 * B2);
+        const double E2 = -(v3 * B1 - v1 * B3);
+        const double E3 = -(v1 * B2 - v2 * B1);
+        const double EE = (E1 * E1 + E2 * E2 + E3 * E3);
+        const double g0 = 1.0 / sqrt(1 - vv);
+        const double d0 = P[0];
+        const double p0 = P[4];
+        const double e0 = p0 / d0 / (gm - 1);
+        const double h0 = 1.0 + e0 + p0 / d0;
+        D[8] = g0 * (g0 - 1) * d0 * h0;
+        D[9] = p0 * (g0 - 1) + d0 * e0 * g0;
+        D[10] = 0.5 * (BB + EE);
+    }
+    D[11] = cs;
+    D[12] = ca;
+    D[13] = Ms;
+    D[14] = Ma;
+    D[15] = s0;
+    D[16] = Bv;
+    return MO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* FieldOperator::volumeIntegratedDiagnostics (FieldOperator.cpp:171-205)    */
+/* over the interior of P with the cell volumes of MeshOperator::measure:    */
+/* the per-zone terms summed in the reference's iteration order (k fastest). */
+/* Dabs (optional) receives the sum of the terms' magnitudes.                */
+/* ------------------------------------------------------------------------ */
+int mo_volume_diagnostics(const mo_config* c, const double* P, double* D, double* Dabs)
+{
+    mgeom g;
+    int err = make_geom(c, &g);
+    const int nd = mo_num_diagnostics(c);
+    if (err) return err;
+    for (int n = 0; n < nd; ++n) {
+        D[n] = 0.0;
+        if (Dabs) Dabs[n] = 0.0;
+    }
+    for (int i = c->ng[0]; i < c->ng[0] + c->ni; ++i)
+        for (int j = c->ng[1]; j < c->ng[1] + c->nj; ++j)
+            for (int k = c->ng[2]; k < c->ng[2] + c->nk; ++k) {
+                double d[17];
+                err = make_diagnostics(c, P + cidx(&g, i, j, k), d);
+                if (err) return err;
+                for (int n = 0; n < nd; ++n) {
+                    D[n] += d[n] * g.dV;
+                    if (Dabs) Dabs[n] += fabs(d[n] * g.dV);
+                }
+            }
+    return MO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* CellCenteredFieldCT::current (CellCenteredFieldCT.cpp:231-257): centred   */
+/* curl of the cell field B (n0, n1, n2, 3); J has the same shape and is     */
+/* zero on the outermost layer of each fleshed axis.                         */
+/* ------------------------------------------------------------------------ */
+void mo_current_cell(const double* B, int n0, int n1, int n2, double h, double* J)
+{
+    const int r = n0 > 1 ? 1 : 0, s = n1 > 1 ? 1 : 0, t = n2 > 1 ? 1 : 0;
+#define BI(i, j, k, c) B[(((long) (i) * n1 + (j)) * n2 + (k)) * 3 + (c)]
+#define JI(i, j, k, c) J[(((long) (i) * n1 + (j)) * n2 + (k)) * 3 + (c)]
+    memset(J, 0, sizeof(double) * (size_t) n0 * n1 * n2 * 3);
+    for (int i = 0; i < n0 - 2 * r; ++i)
+        for (int j = 0; j < n1 - 2 * s; ++j)
+            for (int k = 0; k < n2 - 2 * t; ++k) {
+                const double d0B1 = BI(i + 2 * r, j, k, 1) - BI(i, j, k, 1);
+                const double d0B2 = BI(i + 2 * r, j, k, 2) - BI(i, j, k, 2);
+                const double d1B2 = BI(i, j + 2 * s, k, 2) - BI(i, j, k, 2);
+                const double d1B0 = BI(i, j + 2 * s, k, 0) - BI(i, j, k, 0);
+                const double d2B0 = BI(i, j, k + 2 * t, 0) - BI(i, j, k, 0);
+                const double d2B1 = BI(i, j, k + 2 * t, 1) - BI(i, j, k, 1);
+                JI(i + r, j + s, k + t, 0) = (d1B2 - d2B1) / h / 2;
+                JI(i + r, j + s, k + t, 1) = (d2B0 - d0B2) / h / 2;
+                JI(i + r, j + s, k + t, 2) = (d0B1 - d1B0) / h / 2;
+            }
+#undef BI
+#undef JI
+}

@@ -115,6 +115,18 @@ void mo_ct_correct(double* F, int n0, int n1, int n2, int nq, int ib);
  * shape (n0, n1, n2, 3); M has shape (n0, n1, n2). */
 void mo_monopole_cell(const double* B, int n0, int n1, int n2, double mesh_spacing, double* M);
 
+/* Number of diagnostics ConservationLaw::getDiagnosticNames lists. */
+int mo_num_diagnostics(const mo_config* c);
+
+/* FieldOperator::volumeIntegratedDiagnostics (src/FieldOperator.cpp:171-205)
+ * over the interior of P; D (and Dabs, the sum of the terms' magnitudes, if
+ * not NULL) hold mo_num_diagnostics values. */
+int mo_volume_diagnostics(const mo_config* c, const double* P, double* D, double* Dabs);
+
+/* CellCenteredFieldCT::current (src/CellCenteredFieldCT.cpp:231-257) of cell
+ * data B (n0, n1, n2, 3); J has the same shape. */
+void mo_current_cell(const double* B, int n0, int n1, int n2, double mesh_spacing, double* J);
+
 /* Face-normal unit vectors as CartesianMeshGeometry::faceNormal returns them
  * (UnitVector::xhat/yhat/zhat, src/UnitVector.cpp:9-11,32-39). */
 void mo_face_normals(double n[3][3]);

@@ -127,6 +127,9 @@ class Oracle:
         f("ct_correct").restype = None
         f("monopole_cell").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_double, _D]
         f("monopole_cell").restype = None
+        f("volume_diagnostics").argtypes = [cp, _D, _D, _D]
+        f("current_cell").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_double, _D]
+        f("current_cell").restype = None
         if which == "port":
             L.mo_max_threads.restype = C.c_int
             L.mo_set_threads.argtypes = [C.c_int]
@@ -194,6 +197,23 @@ class Oracle:
         M = np.zeros((n0, n1, n2))
         self._f("monopole_cell")(_ptr(B), n0, n1, n2, h, _ptr(M))
         return M
+
+    def current_cell(self, B: np.ndarray, h: float = 1.0) -> np.ndarray:
+        B = np.ascontiguousarray(B, dtype=float)
+        n0, n1, n2, _ = B.shape
+        J = np.zeros((n0, n1, n2, 3))
+        self._f("current_cell")(_ptr(B), n0, n1, n2, h, _ptr(J))
+        return J
+
+    def volume_diagnostics(self, c: Config, P: np.ndarray):
+        """(status, D, Dabs): FieldOperator::volumeIntegratedDiagnostics over
+        the interior of P, and the sum of the terms' magnitudes (zeros from the
+        reference build, which does not form it)."""
+        nd = 5 if c.law == LAW["hydro"] else 17
+        D, Dabs = np.zeros(nd), np.zeros(nd)
+        status = self._f("volume_diagnostics")(C.byref(c), _ptr(np.ascontiguousarray(P, dtype=float)), _ptr(D),
+                                                _ptr(Dabs))
+        return status, D, Dabs
 
     # -- driver -----------------------------------------------------------------
     def run(self, c: Config, P: np.ndarray, steps: int, cfl: float, t_final: float | None = None,

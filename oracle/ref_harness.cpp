@@ -361,4 +361,35 @@ int mr_vector_potential_to_cell_b (const mo_config* c, const double* Aface, doub
     return status;
 }
 
+int mr_volume_diagnostics (const mo_config* c, const double* P, double* D, double* Dabs)
+{
+    // the drivers' time-series task (e.g. src/Problems/MagneticBraiding.cpp:
+    // 165-166, 205): interior primitives and MeshOperator::measure (cell)
+    int status = MO_OK;
+    mo_failure* fail = nullptr;
+    GUARD_CALL (
+        auto s = make_setup (c);
+        std::memcpy (s.md->P.data(), P, sizeof (double) * s.md->P.size());
+        auto V = s.mo->measure (MeshLocation::cell);
+        auto Pi = s.md->getPrimitive();
+        auto d = s.fo->volumeIntegratedDiagnostics (Pi, V);
+        for (unsigned n = 0; n < d.size(); ++n)
+        {
+            D[n] = d[n];
+            if (Dabs) Dabs[n] = 0.0;
+        }
+    )
+    return status;
+}
+
+void mr_current_cell (const double* B, int n0, int n1, int n2, double h, double* J)
+{
+    auto A = Cow::Array (n0, n1, n2, 3, 1);
+    std::memcpy (A.data(), B, sizeof (double) * A.size());
+    auto ct = CellCenteredFieldCT();
+    ct.setMeshSpacing (h);
+    auto Jc = ct.current (A, MeshLocation::cell);
+    std::memcpy (J, Jc.data(), sizeof (double) * Jc.size());
+}
+
 } // extern "C"

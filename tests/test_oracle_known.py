@@ -78,6 +78,19 @@ def test_field_operator_round_trip_and_courant(port):
     assert st == 0 and dt == 1.0 / 128
 
 
+# TestSuite.cpp:1213-1233: the volume-integrated mass of rho = 1 on the unit
+# interval is the mesh volume, and the first diagnostic is "mass"
+def test_volume_diagnostics_mass_is_mesh_volume(port):
+    from mara2_gb300.solver import diagnostic_names
+    c = O.make_config(law="hydro", shape=(128, 1, 1), ng=0, recon="pcm")
+    c.ng[0] = 0
+    P = np.zeros((128, 1, 1, 5))
+    P[..., 0], P[..., 1] = 1.0, 1.0
+    st, D, _ = port.volume_diagnostics(c, P)
+    assert st == 0 and D[0] == 1.0
+    assert diagnostic_names("hydro")[0] == "mass" and len(diagnostic_names("mhd")) == 17
+
+
 def _divergence(F, dx):
     dA = [dx[1] * dx[2], dx[2] * dx[0], dx[0] * dx[1]]
     dV = dx[0] * dx[1] * dx[2]

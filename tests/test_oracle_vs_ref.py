@@ -142,3 +142,27 @@ def test_workload_vector_potential_matches_reference(ref):
     ref.lib.mr_vector_potential_to_cell_b(C.byref(c), np.ascontiguousarray(A).ctypes.data_as(C.POINTER(C.c_double)),
                                           Bref.ctypes.data_as(C.POINTER(C.c_double)))
     np.testing.assert_allclose(B, Bref, rtol=0, atol=1e-12 * np.abs(Bref).max())
+
+
+@pytest.mark.parametrize("make", [lambda: W.kelvin_helmholtz(24), lambda: W.sod(64),
+                                  lambda: W.mhd_turbulence(8), lambda: W.rmhd_blast(16)])
+def test_volume_diagnostics_bitwise(port, ref, make):
+    """FieldOperator::volumeIntegratedDiagnostics, every law, after a few
+    steps so that velocities and fields are non-trivial."""
+    s, P = make()
+    c = oracle_config(s)
+    for _ in range(2):
+        _, dt = port.courant(c, P)
+        assert port.advance(c, P, 0.0, s.cfl * dt)[0] == 0
+    a = port.volume_diagnostics(c, P)
+    b = ref.volume_diagnostics(c, P)
+    assert a[0] == b[0] == 0
+    assert np.array_equal(_bits(a[1]), _bits(b[1]))
+
+
+def test_current_bitwise(port, ref):
+    """CellCenteredFieldCT::current on 3-D, 2-D and 1-D cell fields."""
+    rng = np.random.default_rng(7)
+    for shape in ((9, 8, 7, 3), (12, 10, 1, 3), (16, 1, 1, 3)):
+        B = rng.normal(size=shape)
+        assert np.array_equal(_bits(port.current_cell(B, 0.1)), _bits(ref.current_cell(B, 0.1)))
