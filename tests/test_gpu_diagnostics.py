@@ -20,7 +20,7 @@ def _stepped(make, port, steps=2):
     c = oracle_config(s)
     for _ in range(steps):
         _, dt = port.courant(c, P)
-        assert port.advance(c, P, 0.0, s.cfl * dt)[0] == 0
+        assert port.advance(c, P, s.cfl * dt)[0] == 0
     return s, P
 
 

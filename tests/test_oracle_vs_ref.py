@@ -153,7 +153,7 @@ def test_volume_diagnostics_bitwise(port, ref, make):
     c = oracle_config(s)
     for _ in range(2):
         _, dt = port.courant(c, P)
-        assert port.advance(c, P, 0.0, s.cfl * dt)[0] == 0
+        assert port.advance(c, P, s.cfl * dt)[0] == 0
     a = port.volume_diagnostics(c, P)
     b = ref.volume_diagnostics(c, P)
     assert a[0] == b[0] == 0
