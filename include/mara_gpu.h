@@ -154,6 +154,48 @@ int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches
  * (the reference's default is 1).  MHD and RMHD only. */
 int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs);
 
+/* ---- source terms ----------------------------------------------------------
+ * MethodOfLinesTVD::setSourceTermsFunction (SolutionSchemes.hpp:36; applied
+ * at SolutionSchemes.cpp:219-228): once per RK stage the scheme evaluates the
+ * source terms S from the stage's primitives and adds them to the flux
+ * divergence L before the RK combine, U = U0 (1 - b) + (U + dt (L + S)) b.
+ * The reference calls a per-cell host function; here the caller's function
+ * is called on the host each time a stage is enqueued (also while a step is
+ * captured into a CUDA graph, whose replays then repeat what it enqueued) and
+ * must enqueue device work on args->stream that writes S, without
+ * synchronising.  A non-zero return ends the call that enqueued the stage
+ * with that status.  Plain FP64 path only (MARA_ERR_CONFIG on a mixed
+ * handle). */
+typedef struct MaraSourceTermsArgs {
+    const double* P;   /* device: the stage's primitives with guards, SoA,
+                          P[q * sP + (k * N[1] + j) * N[0] + i]              */
+    double* S;         /* device: source terms, the same layout; zero until
+                          written; the interior cells are added to L          */
+    long long sP;      /* field stride                                        */
+    int N[3];          /* cells per axis including guards                     */
+    int ng[3];         /* guard cells per axis                                */
+    int nq;            /* fields                                              */
+    double lower[3];   /* the centre of cell (i, j, k) along axis a is
+                          lower[a] + dx[a] * ((i - ng[a]) + 0.5), as
+                          coordinateAtIndex with the start index of
+                          SchemeHelpers::makeFootprint gives it               */
+    double dx[3];
+    double aux[8];     /* the auxiliary data the reference passes (star
+                          particles): zeros                                   */
+    void* stream;      /* the handle's cudaStream_t                           */
+} MaraSourceTermsArgs;
+
+typedef int (*MaraSourceTermsFn)(void* user, const MaraSourceTermsArgs* args);
+
+/* Installs fn (NULL removes it); user is passed back unchanged.  Captured
+ * step graphs are rebuilt on the next run. */
+int mara_gpu_set_source_terms(MaraGpuHandle* h, MaraSourceTermsFn fn, void* user);
+
+/* A ready-made source terms function: a uniform gravitational acceleration
+ * g = ((const double*) user)[0..2], read when the stage is enqueued:
+ * S = (0, rho g1, rho g2, rho g3, rho (v1 g1 + v2 g2 + v3 g3), 0, ...). */
+int mara_source_uniform_gravity(void* user, const MaraSourceTermsArgs* args);
+
 /* Number of volume-integrated diagnostics the law lists
  * (ConservationLaw::getDiagnosticNames, ConservationLaws.cpp:332-341,
  * 576-601, 924-945): 5 for hydro (mass, momentum1-3, total_energy), 17 for

@@ -52,6 +52,15 @@ class MaraGpuStats(C.Structure):
 # Every symbol include/mara_gpu.h declares, with (restype, argtypes).
 _D = C.POINTER(C.c_double)
 _H = C.c_void_p
+class MaraSourceTermsArgs(C.Structure):
+    """MaraSourceTermsArgs (include/mara_gpu.h)."""
+    _fields_ = [("P", C.c_void_p), ("S", C.c_void_p), ("sP", C.c_longlong), ("N", C.c_int * 3),
+                ("ng", C.c_int * 3), ("nq", C.c_int), ("lower", C.c_double * 3), ("dx", C.c_double * 3),
+                ("aux", C.c_double * 8), ("stream", C.c_void_p)]
+
+
+SOURCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(MaraSourceTermsArgs))
+
 SIGNATURES = {
     "mara_gpu_create": (C.c_int, [C.POINTER(MaraGpuConfig), C.POINTER(C.c_void_p)]),
     "mara_gpu_destroy": (C.c_int, [_H]),
@@ -70,6 +79,8 @@ SIGNATURES = {
     "mara_gpu_device_bytes": (C.c_int64, [_H]),
     "mara_gpu_monopole": (C.c_int, [_H, C.c_double, _D]),
     "mara_gpu_num_diagnostics": (C.c_int, [_H]),
+    "mara_gpu_set_source_terms": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
+    "mara_source_uniform_gravity": (C.c_int, [C.c_void_p, C.POINTER(MaraSourceTermsArgs)]),
     "mara_gpu_volume_diagnostics": (C.c_int, [_H, C.c_void_p, C.POINTER(C.c_int)]),
     "mara_gpu_field_diagnostics": (C.c_int, [_H, C.c_double, C.c_void_p]),
     "mara_gpu_status_string": (C.c_char_p, [C.c_int]),

@@ -53,7 +53,8 @@ void plain_flux(int law, int recon, int riemann, int axis, const GridDesc& G, co
                 const double* P, double* F, DevStatus* st, cudaStream_t s);
 void plain_update(int law, const GridDesc& G, const PhysParamsH& pp, const double* Pin, double* Pout,
                   double* U0, double* U, const double* Fx, const double* Fy, const double* Fz,
-                  double b, int stage, const double* dt, DevStatus* st, cudaStream_t s);
+                  double b, int stage, const double* dt, DevStatus* st, cudaStream_t s,
+                  const double* S = nullptr);
 void plain_courant(int law, const GridDesc& G, const PhysParamsH& pp, const double* P, DevStatus* st,
                    cudaStream_t s);
 

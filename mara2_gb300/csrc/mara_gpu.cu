@@ -155,6 +155,10 @@ struct MaraGpuHandle {
     int last_status = 0;
     MaraGpuStats last_stats;
     double* diag = nullptr;              // diagnostics scratch: partial sums, totals, error word
+    MaraSourceTermsFn src_fn = nullptr;  // source terms function (plain path)
+    void* src_user = nullptr;
+    double* S = nullptr;                 // its output, the layout of P
+    int src_error = 0;                   // first non-zero return of src_fn since the last check
 };
 
 static int cuda_status(cudaError_t e)
@@ -172,6 +176,14 @@ static int alloc(MaraGpuHandle* h, void** p, size_t bytes)
     CK(cudaMemsetAsync(*p, 0, bytes, h->stream));
     h->bytes += (int64_t) bytes;
     return MARA_OK;
+}
+
+// the first non-zero status a source terms function returned since the last call
+static int take_source_error(MaraGpuHandle* h)
+{
+    const int e = h->src_error;
+    h->src_error = MARA_OK;
+    return e;
 }
 
 static void timed_begin(MaraGpuHandle* h, int cls, TimedPair& tp)
@@ -265,10 +277,29 @@ static void enqueue_plain_step(MaraGpuHandle* h)
             timed_end(h, tp);
             h->launches++;
         }
+        const double* S = nullptr;
+        if (h->src_fn) {
+            MaraSourceTermsArgs a;
+            std::memset(&a, 0, sizeof(a));
+            a.P = h->P[h->cur];
+            a.S = h->S;
+            a.sP = h->G.sP;
+            a.nq = h->G.nq;
+            for (int ax = 0; ax < 3; ++ax) {
+                a.N[ax] = h->G.N[ax];
+                a.ng[ax] = h->G.g[ax];
+                a.lower[ax] = c.lower[ax];
+                a.dx[ax] = (c.upper[ax] - c.lower[ax]) / (ax == 0 ? c.ni : ax == 1 ? c.nj : c.nk);
+            }
+            a.stream = (void*) h->stream;
+            const int rc = h->src_fn(h->src_user, &a);
+            if (rc != MARA_OK && h->src_error == MARA_OK) h->src_error = rc;
+            S = h->S;
+        }
         TimedPair tp;
         timed_begin(h, 1, tp);
         plain_update(c.law, h->G, h->pp, h->P[h->cur], h->P[1 - h->cur], h->U0, h->U, h->F[0], h->F[1], h->F[2],
-                     b[rk], rk, &h->st->dt, h->st, h->stream);
+                     b[rk], rk, &h->st->dt, h->st, h->stream, S);
         timed_end(h, tp);
         h->launches++;
         h->cur = 1 - h->cur;
@@ -392,6 +423,7 @@ int mara_gpu_destroy(MaraGpuHandle* h)
     cudaFree(h->stage_aos);
     cudaFree(h->st);
     cudaFree(h->diag);
+    cudaFree(h->S);
     if (h->mixed) mixed_destroy(h->mixed);
     if (h->st_host) cudaFreeHost(h->st_host);
     for (int e = 0; e < 17; ++e) if (h->ev[e]) cudaEventDestroy(h->ev[e]);
@@ -472,6 +504,7 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
         launch_set_dt(h->st, dt, h->stream);
         h->launches++;
         enqueue_step(h);
+        if (const int se = take_source_error(h)) return se;
     }
     h->steps++;
     return cuda_status(cudaGetLastError());
@@ -520,6 +553,12 @@ static int build_run_graph(MaraGpuHandle* h, int which, double cfl, double t_fin
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_run_step(h, cfl, t_final);
     CK(cudaStreamEndCapture(h->stream, &g));
+    if (const int se = take_source_error(h)) {
+        cudaGraphDestroy(g);
+        h->timing = timing;
+        h->launches = launches;
+        return se;
+    }
     h->timing = timing;
     h->launches = launches;
     if (h->graph[which]) cudaGraphExecDestroy(h->graph[which]);
@@ -553,9 +592,9 @@ static int enqueue_run(MaraGpuHandle* h, int max_steps, double cfl, double t_fin
                 const int cur0 = h->cur;
                 const int par0 = h->mixed ? mixed_parity(h->mixed) : 0;
                 int rc = build_run_graph(h, which, cfl, t_final);
-                if (rc) return rc;
                 h->cur = cur0;
                 if (h->mixed) mixed_set_parity(h->mixed, par0);
+                if (rc) return rc;
             }
             CK(cudaGraphLaunch(h->graph[which], h->stream));
             // advance the host-side parity exactly as the captured step did
@@ -564,6 +603,7 @@ static int enqueue_run(MaraGpuHandle* h, int max_steps, double cfl, double t_fin
             h->launches += launches_per_run_step(h);
         } else {
             enqueue_run_step(h, cfl, t_final);
+            if (const int se = take_source_error(h)) return se;
         }
         h->steps++;
     }
@@ -676,6 +716,24 @@ int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs)
     CK(cudaMemcpyAsync(&bits, out, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     *max_abs = __builtin_bit_cast(double, bits);
+    return MARA_OK;
+}
+
+int mara_gpu_set_source_terms(MaraGpuHandle* h, MaraSourceTermsFn fn, void* user)
+{
+    if (!h) return MARA_ERR_ARGUMENT;
+    if (h->mixed) return fn ? MARA_ERR_CONFIG : MARA_OK;
+    CK(cudaSetDevice(h->cfg.device));
+    if (fn && !h->S) {
+        const size_t bytes = (size_t) h->G.sP * h->G.nq * sizeof(double);
+        if (alloc(h, (void**) &h->S, bytes)) return MARA_ERR_CUDA;
+    }
+    h->src_fn = fn;
+    h->src_user = user;
+    h->src_error = MARA_OK;
+    // the captured step graphs hold what the previous function enqueued
+    for (int g = 0; g < 2; ++g)
+        if (h->graph[g]) { cudaGraphExecDestroy(h->graph[g]); h->graph[g] = nullptr; }
     return MARA_OK;
 }
 

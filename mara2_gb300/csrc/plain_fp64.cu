@@ -23,6 +23,7 @@
 //                       so every guard zone equals one interior zone (velocity
 //                       components negated on reflecting axes) and the zone
 //                       that owns a value writes all of its guard images.
+#include "../../include/mara_gpu.h"
 #include "internal.h"
 #include "physics_fp64.cuh"
 
@@ -164,7 +165,8 @@ template <int LAW>
 __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ Pin, double* __restrict__ Pout,
                                                      double* __restrict__ U0, double* __restrict__ U,
                                                      FluxView V, GridDesc G, PhysParams pp, double b, int stage,
-                                                     const double* __restrict__ dtp, DevStatus* __restrict__ st)
+                                                     const double* __restrict__ dtp, DevStatus* __restrict__ st,
+                                                     const double* __restrict__ S)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     if (st->code != 0 || st->halt || st->done) return;
@@ -203,8 +205,9 @@ __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ 
         const double fym = fy ? face_flux<NQ>(V, G, 1, q, i, j, k) : 0.0;
         const double fzp = fz ? face_flux<NQ>(V, G, 2, q, i, j, k + 1) : 0.0;
         const double fzm = fz ? face_flux<NQ>(V, G, 2, q, i, j, k) : 0.0;
-        const double L = factor / vol * (+fxp * A1000 - fxm * A0000 + fyp * A0101 - fym * A0001
-                                         + fzp * A0012 - fzm * A0002);
+        double L = factor / vol * (+fxp * A1000 - fxm * A0000 + fyp * A0101 - fym * A0001
+                                   + fzp * A0012 - fzm * A0002);
+        if (S) L += S[q * G.sP + pc];  // the source terms function's array (SolutionSchemes.cpp:219-228)
         Un[q] = Uo[q] * (1 - b) + (Up[q] + dt * L) * b;
         U[q * G.sU + uc] = Un[q];
     }
@@ -358,7 +361,7 @@ void plain_flux(int law, int recon, int riemann, int axis, const GridDesc& G, co
 
 void plain_update(int law, const GridDesc& G, const PhysParamsH& ph, const double* Pin, double* Pout,
                   double* U0, double* U, const double* Fx, const double* Fy, const double* Fz,
-                  double b, int stage, const double* dt, DevStatus* st, cudaStream_t s)
+                  double b, int stage, const double* dt, DevStatus* st, cudaStream_t s, const double* S)
 {
     const PhysParams pp = to_dev(ph);
     FluxView V;
@@ -368,9 +371,9 @@ void plain_update(int law, const GridDesc& G, const PhysParamsH& ph, const doubl
     V.M1 = G.N[1] + 1;
     dim3 block(128), grid((G.n[0] + 127) / 128, G.n[1], G.n[2]);
     switch (law) {
-        case LAW_HYDRO: update_kernel<LAW_HYDRO><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st); break;
-        case LAW_MHD: update_kernel<LAW_MHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st); break;
-        default: update_kernel<LAW_RMHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st); break;
+        case LAW_HYDRO: update_kernel<LAW_HYDRO><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
+        case LAW_MHD: update_kernel<LAW_MHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
+        default: update_kernel<LAW_RMHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
     }
 }
 
@@ -387,3 +390,29 @@ void plain_courant(int law, const GridDesc& G, const PhysParamsH& ph, const doub
 }
 
 } // namespace mara
+
+// ---------------------------------------------------------------------------
+// The ready-made uniform-gravity source terms function (include/mara_gpu.h).
+__global__ void k_uniform_gravity(const double* __restrict__ P, double* __restrict__ S, long long sP, long long cells,
+                                  int nq, double g1, double g2, double g3)
+{
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    const double rho = P[c], v1 = P[sP + c], v2 = P[2 * sP + c], v3 = P[3 * sP + c];
+    S[c] = 0.0;
+    S[sP + c] = rho * g1;
+    S[2 * sP + c] = rho * g2;
+    S[3 * sP + c] = rho * g3;
+    S[4 * sP + c] = rho * (v1 * g1 + v2 * g2 + v3 * g3);
+    for (int q = 5; q < nq; ++q) S[q * sP + c] = 0.0;
+}
+
+extern "C" int mara_source_uniform_gravity(void* user, const MaraSourceTermsArgs* a)
+{
+    if (!user || !a) return MARA_ERR_ARGUMENT;
+    const double* g = (const double*) user;
+    const long long cells = (long long) a->N[0] * a->N[1] * a->N[2];
+    k_uniform_gravity<<<(unsigned) ((cells + 255) / 256), 256, 0, (cudaStream_t) a->stream>>>(
+        a->P, a->S, a->sP, cells, a->nq, g[0], g[1], g[2]);
+    return cudaGetLastError() == cudaSuccess ? MARA_OK : MARA_ERR_CUDA;
+}

@@ -139,6 +139,27 @@ class Solver:
     def set_kernel_timing(self, on: bool) -> None:
         self.lib.mara_gpu_set_kernel_timing(self.h, int(on))
 
+    def set_source_terms(self, fn=None, gravity=None) -> None:
+        """MethodOfLinesTVD::setSourceTermsFunction on the plain path:
+        gravity=(g1, g2, g3) installs the library's uniform-gravity source; fn
+        is a MaraSourceTermsFn (a ctypes function pointer or a Python callable
+        (user, args) -> status that enqueues device work on args.stream);
+        neither removes the source terms."""
+        self._src_keep = None
+        if gravity is not None:
+            g = (C.c_double * 3)(*[float(v) for v in gravity])
+            fptr = C.cast(self.lib.mara_source_uniform_gravity, C.c_void_p)
+            self._src_keep = (g,)
+            N.check(self.lib.mara_gpu_set_source_terms(self.h, fptr, C.cast(g, C.c_void_p)),
+                    "mara_gpu_set_source_terms")
+        elif fn is not None:
+            cb = fn if isinstance(fn, N.SOURCE_FN) else N.SOURCE_FN(fn)
+            self._src_keep = (cb,)
+            N.check(self.lib.mara_gpu_set_source_terms(self.h, C.cast(cb, C.c_void_p), None),
+                    "mara_gpu_set_source_terms")
+        else:
+            N.check(self.lib.mara_gpu_set_source_terms(self.h, None, None), "mara_gpu_set_source_terms")
+
     def volume_diagnostics(self) -> dict:
         """FieldOperator::volumeIntegratedDiagnostics of the resident state,
         by the names ConservationLaw::getDiagnosticNames gives them."""

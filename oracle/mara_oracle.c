@@ -1200,6 +1200,45 @@ int mo_courant(const mo_config* c, const double* P, double* dt_out)
 /* ------------------------------------------------------------------------ */
 /* MethodOfLinesTVD::advance (SolutionSchemes.cpp:108-275)                   */
 /* ------------------------------------------------------------------------ */
+/* ------------------------------------------------------------------------ */
+/* MethodOfLinesTVD::setSourceTermsFunction (SolutionSchemes.hpp:36) and     */
+/* MeshOperator::generateSourceTerms (MeshOperator.cpp:197-218): a per-cell  */
+/* function of the cell centre, the auxiliary data (zeros: no star           */
+/* particles) and the primitives, evaluated over every cell of the array     */
+/* with guards and added to L (SolutionSchemes.cpp:219-228)                  */
+/* ------------------------------------------------------------------------ */
+static mo_source_fn g_src_fn = NULL;
+static void* g_src_user = NULL;
+
+void mo_set_source_terms(mo_source_fn fn, void* user)
+{
+    g_src_fn = fn;
+    g_src_user = user;
+}
+
+static void add_source_terms(const mo_config* c, const mgeom* g, const double* P, double* L)
+{
+    static const double aux[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < g->N[0]; ++i)
+        for (int j = 0; j < g->N[1]; ++j)
+            for (int k = 0; k < g->N[2]; ++k) {
+                /* CartesianMeshGeometry::coordinateAtIndex (CartesianMeshGeometry.
+                 * cpp:61-67) at the index plus the start index -ng of
+                 * SchemeHelpers::makeFootprint */
+                const double x = c->lower[0] + g->dx[0] * ((double) (i - c->ng[0]) + 0.5);
+                const double y = c->lower[1] + g->dx[1] * ((double) (j - c->ng[1]) + 0.5);
+                const double z = c->lower[2] + g->dx[2] * ((double) (k - c->ng[2]) + 0.5);
+                double p[NSLOT], S[NSLOT];
+                const long o = cidx(g, i, j, k);
+                for (int q = 0; q < NSLOT; ++q) {
+                    p[q] = q < g->nq ? P[o + q] : 0.0;
+                    S[q] = 0.0;
+                }
+                g_src_fn(g_src_user, x, y, z, aux, p, S);
+                for (int q = 0; q < g->nq; ++q) L[o + q] += S[q];
+            }
+}
+
 int mo_advance(const mo_config* c, double* P, double t0, double dt, mo_failure* fail)
 {
     static const double b1[1] = {1.0};
@@ -1252,6 +1291,8 @@ int mo_advance(const mo_config* c, double* P, double t0, double dt, mo_failure* 
                                 + F[fidx(&g, i, j, k + 1, q, 2)] * A0012
                                 - F[fidx(&g, i, j, k, q, 2)] * A0002);
         }
+
+        if (g_src_fn) add_source_terms(c, &g, P, L);
 
         /* RK combine over every element (SolutionSchemes.cpp:232-235) */
         {

@@ -78,6 +78,13 @@ typedef struct mo_failure {
 int mo_num_fields(const mo_config* c);
 int mo_stencil_size(const mo_config* c);
 
+/* Source terms function (MethodOfLinesTVD::setSourceTermsFunction): cell
+ * centre, auxiliary data, primitives (MARA_NUM_FIELDS slots) -> source terms
+ * added to L.  NULL removes it.  Applies to every later mo_advance. */
+typedef void (*mo_source_fn)(void* user, double x, double y, double z, const double aux[8], const double* P,
+                             double* S);
+void mo_set_source_terms(mo_source_fn fn, void* user);
+
 /* MethodOfLinesTVD::advance (src/SolutionSchemes.cpp:108-275) on the AoS
  * array P (with guards), in place. */
 int mo_advance(const mo_config* c, double* P, double t0, double dt, mo_failure* fail);

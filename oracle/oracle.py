@@ -36,6 +36,10 @@ ERR_GUARD_TOO_SMALL = 19
 ERR_CONFIG = 20
 
 
+SOURCE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double),
+                        C.POINTER(C.c_double), C.POINTER(C.c_double))
+
+
 class Config(C.Structure):
     """Mirror of ``mo_config`` in mara_oracle.h."""
 
@@ -127,6 +131,9 @@ class Oracle:
         f("ct_correct").restype = None
         f("monopole_cell").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_double, _D]
         f("monopole_cell").restype = None
+        f("set_source_terms").argtypes = [C.c_void_p, C.c_void_p]
+        f("set_source_terms").restype = None
+        self._src = None
         f("volume_diagnostics").argtypes = [cp, _D, _D, _D]
         f("current_cell").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_double, _D]
         f("current_cell").restype = None
@@ -197,6 +204,23 @@ class Oracle:
         M = np.zeros((n0, n1, n2))
         self._f("monopole_cell")(_ptr(B), n0, n1, n2, h, _ptr(M))
         return M
+
+    def set_source_terms(self, fn=None):
+        """MethodOfLinesTVD::setSourceTermsFunction for later advances:
+        fn(x, y, z, aux, P) -> S, with P and S of MARA_NUM_FIELDS (10) slots;
+        None removes it."""
+        if fn is None:
+            self._src = None
+            self._f("set_source_terms")(None, None)
+            return
+
+        def tramp(user, x, y, z, aux, P, S):
+            out = fn(x, y, z, [aux[n] for n in range(8)], [P[n] for n in range(10)])
+            for q, v in enumerate(out):
+                S[q] = v
+
+        self._src = SOURCE_FN(tramp)
+        self._f("set_source_terms")(C.cast(self._src, C.c_void_p), None)
 
     def current_cell(self, B: np.ndarray, h: float = 1.0) -> np.ndarray:
         B = np.ascontiguousarray(B, dtype=float)

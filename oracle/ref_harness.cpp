@@ -82,6 +82,11 @@ private:
 };
 
 // ----------------------------------------------------------------------------
+// The source terms function every later setup installs (mr_set_source_terms)
+static mo_source_fn g_src_fn = nullptr;
+static void* g_src_user = nullptr;
+
+// ----------------------------------------------------------------------------
 struct Setup
 {
     std::shared_ptr<CartesianMeshGeometry> mg;
@@ -152,6 +157,15 @@ static Setup make_setup (const mo_config* c)
     s.ss->setMeshOperator (s.mo);
     s.ss->setBoundaryCondition (s.bc);
     s.ss->setIntercellFluxScheme (s.fs);
+    if (g_src_fn)
+    {
+        s.ss->setSourceTermsFunction ([] (double x, double y, double z, std::array<double, 8> t, StateArray P)
+        {
+            auto S = StateArray();
+            g_src_fn (g_src_user, x, y, z, t.data(), P.data(), S.data());
+            return S;
+        });
+    }
 
     s.md = std::make_shared<MeshData> (cs, bs, s.nq);
     return s;
@@ -359,6 +373,12 @@ int mr_vector_potential_to_cell_b (const mo_config* c, const double* Aface, doub
         std::memcpy (Bcell, B.data(), sizeof (double) * B.size());
     )
     return status;
+}
+
+void mr_set_source_terms (mo_source_fn fn, void* user)
+{
+    g_src_fn = fn;
+    g_src_user = user;
 }
 
 int mr_volume_diagnostics (const mo_config* c, const double* P, double* D, double* Dabs)

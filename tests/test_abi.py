@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared(header):
     text = open(os.path.join(ROOT, "include", header)).read()
-    return sorted(set(re.findall(r"\b(mara_gpu_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mara_(?:gpu|source)_\w+)\s*\(", text)))
 
 
 def _declared_batch():

@@ -166,3 +166,38 @@ def test_current_bitwise(port, ref):
     for shape in ((9, 8, 7, 3), (12, 10, 1, 3), (16, 1, 1, 3)):
         B = rng.normal(size=shape)
         assert np.array_equal(_bits(port.current_cell(B, 0.1)), _bits(ref.current_cell(B, 0.1)))
+
+
+def _gravity(g):
+    def S(x, y, z, aux, P):
+        rho = P[0]
+        return [0.0, rho * g[0], rho * g[1], rho * g[2], rho * (P[1] * g[0] + P[2] * g[1] + P[3] * g[2])] + [0.0] * 5
+    return S
+
+
+def _position_source(x, y, z, aux, P):
+    # depends on the cell centre, so the coordinates are checked too
+    return [0.0, x * y, -z + x, 0.0, P[0] * x] + [0.0] * 5
+
+
+@pytest.mark.parametrize("make,src", [(lambda: W.kelvin_helmholtz(16), _gravity((0.0, -1.0, 0.0))),
+                                      (lambda: W.sod(48), _position_source),
+                                      (lambda: W.mhd_turbulence(6), _gravity((0.3, -0.2, 0.1)))])
+def test_source_terms_bitwise(port, ref, make, src):
+    """MethodOfLinesTVD::setSourceTermsFunction: S from the stage's
+    primitives and the cell centres, added to L before the RK combine."""
+    s, P = make()
+    c = oracle_config(s)
+    A, B = P.copy(), P.copy()
+    try:
+        port.set_source_terms(src)
+        ref.set_source_terms(src)
+        for _ in range(2):
+            _, dt = port.courant(c, A)
+            assert port.advance(c, A, s.cfl * dt)[0] == 0
+            assert ref.advance(c, B, s.cfl * dt)[0] == 0
+    finally:
+        port.set_source_terms(None)
+        ref.set_source_terms(None)
+    assert np.array_equal(_bits(A), _bits(B))
+    assert not np.array_equal(_bits(A), _bits(P))
