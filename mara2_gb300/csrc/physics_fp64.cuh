@@ -56,6 +56,26 @@ template <int NQ> struct StateD {
     double P[NQ], U[NQ], F[NQ], A[NQ];
 };
 
+// IEEE comparison of doubles done on their bit patterns (integer pipe): the
+// FP64 pipe of this GPU runs at 1/64 of the FP32 rate and a compare takes a
+// slot there like a multiply.  Mapping a double to sign ? -|bits| : |bits|
+// orders every non-NaN value, with -0 and +0 equal; a NaN operand makes the
+// comparison false, as in IEEE arithmetic.  (Measured: it pays in the
+// Courant reduction and in minmod, not in the Riemann solvers' slot max/min.)
+__device__ __forceinline__ long long dkey(long long b)
+{
+    const long long m = b & 0x7fffffffffffffffll;
+    return b < 0 ? -m : m;
+}
+
+__device__ __forceinline__ bool dnan(long long b) { return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll; }
+
+__device__ __forceinline__ bool dlt(double a, double b)  // a < b
+{
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return !dnan(x) && !dnan(y) && dkey(x) < dkey(y);
+}
+
 __device__ __forceinline__ double dmin2(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double dmax2(double a, double b) { return a > b ? a : b; }
 __device__ __forceinline__ double dmin3(double a, double b, double c) { return a < b ? dmin2(a, c) : dmin2(b, c); }
@@ -609,13 +629,42 @@ __device__ __forceinline__ int law_cons(const PhysParams& pp, const double* U, d
 // Reconstruction (Reconstruction.cpp:55-169)
 __device__ __forceinline__ int dsgn(double x) { return (x > 0) - (x < 0); }
 
+// The sign tests, MIN3 and the small factor 0.25 |SGN(a) + SGN(b)| (SGN(a) +
+// SGN(c)) of the generalised minmod are done on the bit patterns, so that
+// only the arithmetic reaches the FP64 pipe (a compare costs as much there as
+// a multiply); the results are the reference's bit for bit:
+//  * SGN(x) = (x > 0) - (x < 0) is 0 for +-0 and NaN;
+//  * for |x|, |y| (sign bit clear) x < y is false when either is NaN and is
+//    otherwise the order of the bit patterns;
+//  * with s = SGN(a) + SGN(b) and t = SGN(a) + SGN(c) in -2..2, the product
+//    (0.25 |s|) t is exactly 0, 0.25, 0.5 or 1 in magnitude (0.25 |s| |t|)
+//    and carries the sign bit exactly when t < 0 (a zero times a negative t
+//    is -0), so its bits are assembled directly; the last factor, times
+//    MIN3, is the reference's multiply on the same operands.
+__device__ __forceinline__ int bsgn(long long b)
+{
+    const long long m = b & 0x7fffffffffffffffll;
+    return (m == 0 || m > 0x7ff0000000000000ll) ? 0 : (b < 0 ? -1 : 1);
+}
+
 __device__ __forceinline__ double minmod(double theta, double ul, double u0, double ur)
 {
     const double a = theta * (u0 - ul);
     const double b = 0.5 * (ur - ul);
     const double c = theta * (ur - u0);
-    return 0.25 * fabs((double) (dsgn(a) + dsgn(b))) * (double) (dsgn(a) + dsgn(c))
-         * dmin3(fabs(a), fabs(b), fabs(c));
+    const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b), bc = __double_as_longlong(c);
+    const int sa = bsgn(ba), sb = bsgn(bb), sc = bsgn(bc);
+    const int s = sa + sb, t = sa + sc;
+    const int p = (s < 0 ? -s : s) * (t < 0 ? -t : t);  // 0, 1, 2 or 4
+    const long long mag = p == 0 ? 0ll : p == 1 ? 0x3fd0000000000000ll : p == 2 ? 0x3fe0000000000000ll
+                                                                        : 0x3ff0000000000000ll;
+    const double k = __longlong_as_double(mag | (t < 0 ? (long long) 0x8000000000000000ull : 0ll));
+    // MIN3(|a|, |b|, |c|) = |a| < |b| ? MIN2(|a|, |c|) : MIN2(|b|, |c|)
+    const long long INF = 0x7ff0000000000000ll;
+    const long long xa = ba & 0x7fffffffffffffffll, xb = bb & 0x7fffffffffffffffll, xc = bc & 0x7fffffffffffffffll;
+    auto lt = [INF](long long x, long long y) { return x < y && y <= INF; };
+    const long long m = lt(xa, xb) ? (lt(xa, xc) ? xa : xc) : (lt(xb, xc) ? xb : xc);
+    return k * __longlong_as_double(m);
 }
 
 #define MARA_SQU(x) ((x) * (x))
@@ -751,7 +800,7 @@ __device__ __forceinline__ double max_eigen_magnitude(const double* A)
     double m = 0.0;
 #pragma unroll
     for (int n = 0; n < NQ; ++n)
-        if (m < fabs(A[n])) m = fabs(A[n]);
+        if (dlt(m, fabs(A[n]))) m = fabs(A[n]);
     return m;
 }
 
