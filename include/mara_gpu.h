@@ -104,7 +104,13 @@ typedef struct MaraGpuHandle MaraGpuHandle;
 int mara_gpu_create(const MaraGpuConfig* config, MaraGpuHandle** handle);
 int mara_gpu_destroy(MaraGpuHandle* handle);
 
-/* Host <-> device copies of MeshData::P (with guards, AoS FP64). */
+/* Host <-> device copies of MeshData::P (with guards, AoS FP64).  A
+ * page-locked array (cudaHostAlloc / cudaHostRegister) is read or written
+ * in place by the layout-conversion kernels over the chip-to-chip link; a
+ * pageable one goes through a device staging buffer in chunks.  upload may
+ * still be reading the array when it returns: the next call that
+ * synchronises the handle (download, synchronize, courant, run, stats)
+ * marks the end. */
 int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos);
 int mara_gpu_download(MaraGpuHandle* h, double* P_aos);
 

@@ -68,28 +68,49 @@ __global__ void k_run_begin(DevStatus* st, double t)
 
 // AoS (i, j, k, q), q fastest  <->  SoA q * sP + (k * N1 + j) * N0 + i, over
 // the AoS cells [c0, c1)
-__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, GridDesc G, long long c0,
-                             long long c1)
+// AoS (k fastest, the reference's MeshData::P) <-> SoA (x fastest).  A
+// block's cells are one contiguous slab of the AoS array, moved with
+// consecutive threads on consecutive doubles (the array may be the caller's
+// page-locked host memory, reached over the chip-to-chip link) and
+// transposed in shared memory.
+constexpr int CONV_BLOCK = 256;
+constexpr int CONV_MAXQ = 8;
+
+__device__ __forceinline__ long long soa_index(long long c, const GridDesc& G)
 {
-    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x; // AoS cell order
-    if (c >= c1) return;
     const int k = (int) (c % G.N[2]);
     const int j = (int) ((c / G.N[2]) % G.N[1]);
     const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
-    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    for (int q = 0; q < G.nq; ++q) soa[q * G.sP + s] = aos[c * G.nq + q];
+    return ((long long) k * G.N[1] + j) * G.N[0] + i;
 }
 
-__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos, GridDesc G, long long c0,
-                             long long c1)
+__global__ void __launch_bounds__(CONV_BLOCK) k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa,
+                                                           GridDesc G, long long c0, long long c1)
 {
-    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= c1) return;
-    const int k = (int) (c % G.N[2]);
-    const int j = (int) ((c / G.N[2]) % G.N[1]);
-    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
-    const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    for (int q = 0; q < G.nq; ++q) aos[c * G.nq + q] = soa[q * G.sP + s];
+    __shared__ double slab[CONV_BLOCK * CONV_MAXQ];
+    const int nq = G.nq;
+    const long long b0 = c0 + blockIdx.x * (long long) CONV_BLOCK;
+    const int nc = (int) min((long long) CONV_BLOCK, c1 - b0);
+    for (int e = threadIdx.x; e < nc * nq; e += CONV_BLOCK) slab[e] = aos[b0 * nq + e];
+    __syncthreads();
+    if (threadIdx.x >= nc) return;
+    const long long s = soa_index(b0 + threadIdx.x, G);
+    for (int q = 0; q < nq; ++q) soa[q * G.sP + s] = slab[threadIdx.x * nq + q];
+}
+
+__global__ void __launch_bounds__(CONV_BLOCK) k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos,
+                                                           GridDesc G, long long c0, long long c1)
+{
+    __shared__ double slab[CONV_BLOCK * CONV_MAXQ];
+    const int nq = G.nq;
+    const long long b0 = c0 + blockIdx.x * (long long) CONV_BLOCK;
+    const int nc = (int) min((long long) CONV_BLOCK, c1 - b0);
+    if (threadIdx.x < nc) {
+        const long long s = soa_index(b0 + threadIdx.x, G);
+        for (int q = 0; q < nq; ++q) slab[threadIdx.x * nq + q] = soa[q * G.sP + s];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nc * nq; e += CONV_BLOCK) aos[b0 * nq + e] = slab[e];
 }
 
 void launch_courant_init(DevStatus* st, cudaStream_t s) { k_courant_init<<<1, 1, 0, s>>>(st); }
@@ -103,13 +124,13 @@ void launch_aos_to_soa_range(const double* aos, double* soa, const GridDesc& G, 
                              cudaStream_t s)
 {
     if (c1 <= c0) return;
-    k_aos_to_soa<<<(unsigned) ((c1 - c0 + 255) / 256), 256, 0, s>>>(aos, soa, G, c0, c1);
+    k_aos_to_soa<<<(unsigned) ((c1 - c0 + CONV_BLOCK - 1) / CONV_BLOCK), CONV_BLOCK, 0, s>>>(aos, soa, G, c0, c1);
 }
 void launch_soa_to_aos_range(const double* soa, double* aos, const GridDesc& G, long long c0, long long c1,
                              cudaStream_t s)
 {
     if (c1 <= c0) return;
-    k_soa_to_aos<<<(unsigned) ((c1 - c0 + 255) / 256), 256, 0, s>>>(soa, aos, G, c0, c1);
+    k_soa_to_aos<<<(unsigned) ((c1 - c0 + CONV_BLOCK - 1) / CONV_BLOCK), CONV_BLOCK, 0, s>>>(soa, aos, G, c0, c1);
 }
 void launch_aos_to_soa(const double* aos, double* soa, const GridDesc& G, cudaStream_t s)
 {
@@ -443,6 +464,21 @@ static int chunks_of(const MaraGpuHandle* h)
     return 8;
 }
 
+// The device address of a page-locked host array (cudaHostAlloc /
+// cudaHostRegister), or null for pageable memory.  On this platform the GPU
+// reaches page-locked host memory over the chip-to-chip link, so the layout
+// conversion kernels can read or write the caller's array directly: the copy
+// and the conversion are one pass, at the link's bandwidth.
+static const void* direct_host_pointer(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;
@@ -452,6 +488,14 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
     k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
     h->launches++;
     if (h->mixed) mixed_load_begin(h->mixed, h->stream);
+    if (const double* d = (const double*) direct_host_pointer(P_aos)) {
+        const long long cells = h->G.sP;
+        if (h->mixed) mixed_load_aos_range(h->mixed, d, 0, cells, h->st, h->stream);
+        else launch_aos_to_soa_range(d, h->P[h->cur], h->G, 0, cells, h->stream);
+        h->launches++;
+        if (h->mixed) mixed_load_finish(h->mixed, h->st, h->stream);
+        return cuda_status(cudaGetLastError());
+    }
     const int C = chunks_of(h);
     const long long cells = h->G.sP, nq = h->G.nq;
     CK(cudaEventRecord(h->ev[16], h->stream));
@@ -474,6 +518,14 @@ int mara_gpu_download(MaraGpuHandle* h, double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    if (double* d = (double*) direct_host_pointer(P_aos)) {
+        const long long cells = h->G.sP;
+        if (h->mixed) mixed_store_aos_range(h->mixed, d, 0, cells, h->stream);
+        else launch_soa_to_aos_range(h->P[h->cur], d, h->G, 0, cells, h->stream);
+        h->launches++;
+        CK(cudaStreamSynchronize(h->stream));
+        return cuda_status(cudaGetLastError());
+    }
     const int C = chunks_of(h);
     const long long cells = h->G.sP, nq = h->G.nq;
     for (int k = 0; k < C; ++k) {

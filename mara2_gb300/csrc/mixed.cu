@@ -304,20 +304,33 @@ __global__ void __launch_bounds__(256) courant_f_kernel(const float* __restrict_
 // on the general form, FP32 primitives with guards.  Hydro converts with one
 // reciprocal instead of FP64 divisions (FP64 is slow on this GPU) and, when
 // cfl is given, reduces the Courant step of the loaded zones on the way.
+//
+// A block's cells are one contiguous slab of the AoS array: it is read with
+// consecutive threads on consecutive doubles (the array may be the caller's
+// page-locked host memory, read over the chip-to-chip link, where scattered
+// per-cell accesses are slow) and transposed to cells in shared memory.
+constexpr int CONV_BLOCK = 256;
+
 template <int LAW>
-__global__ void load_kernel(const double* __restrict__ aos, long long c0, long long c1, float* Uh, float* Ul,
-                            float* Pf, GridF G, PhysParams pp, DevStatus* st, unsigned long long* cfl)
+__global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restrict__ aos, long long c0, long long c1,
+                                                          float* Uh, float* Ul, float* Pf, GridF G, PhysParams pp,
+                                                          DevStatus* st, unsigned long long* cfl)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    __shared__ double slab[CONV_BLOCK * NQ];
+    const long long b0 = c0 + blockIdx.x * (long long) CONV_BLOCK;
+    const int nc = (int) min((long long) CONV_BLOCK, c1 - b0);
+    for (int e = threadIdx.x; e < nc * NQ; e += CONV_BLOCK) slab[e] = aos[b0 * NQ + e];
+    __syncthreads();
+    const long long c = b0 + threadIdx.x;
     float zdt = 3.0e38f;
-    if (c < c1) {
+    if (threadIdx.x < nc) {
         const int k = (int) (c % G.N[2]);
         const int j = (int) ((c / G.N[2]) % G.N[1]);
         const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
         double P[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) P[q] = aos[c * NQ + q];
+        for (int q = 0; q < NQ; ++q) P[q] = slab[threadIdx.x * NQ + q];
         const long long s = ((long long) k * G.N[1] + j) * G.N[0] + i;
         if (Pf)
 #pragma unroll
@@ -349,15 +362,13 @@ __global__ void load_kernel(const double* __restrict__ aos, long long c0, long l
     if (cfl) block_min_to(cfl, zdt);
 }
 
-// FP32-pair state -> AoS FP64 primitives with guards (cells [c0, c1); the
-// guard zones are boundary images of interior zones)
+// FP64 primitives of cell c (AoS order) from the FP32-pair state; a guard
+// zone is the boundary image of an interior zone
 template <int LAW>
-__global__ void store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos, long long c0, long long c1,
-                             GridF G, PhysParams pp)
+__device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, long long c, const GridF& G,
+                                           const PhysParams& pp, double* out)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
-    const long long c = c0 + blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= c1) return;
     const int k = (int) (c % G.N[2]);
     const int j = (int) ((c / G.N[2]) % G.N[1]);
     const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
@@ -379,7 +390,22 @@ __global__ void store_kernel(const float* Uh, const float* Ul, double* __restric
     if (f[1]) P[2] = -P[2];
     if (f[2]) P[3] = -P[3];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) aos[c * NQ + q] = P[q];
+    for (int q = 0; q < NQ; ++q) out[q] = P[q];
+}
+
+// FP32-pair state -> AoS FP64 primitives with guards, cells [c0, c1), each
+// block's slab written as one contiguous run
+template <int LAW>
+__global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos,
+                                                           long long c0, long long c1, GridF G, PhysParams pp)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    __shared__ double slab[CONV_BLOCK * NQ];
+    const long long b0 = c0 + blockIdx.x * (long long) CONV_BLOCK;
+    const int nc = (int) min((long long) CONV_BLOCK, c1 - b0);
+    if (threadIdx.x < nc) store_cell<LAW>(Uh, Ul, b0 + threadIdx.x, G, pp, &slab[threadIdx.x * NQ]);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nc * NQ; e += CONV_BLOCK) aos[b0 * NQ + e] = slab[e];
 }
 
 __global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long long) __double_as_longlong(DBL_MAX); }

@@ -150,3 +150,29 @@ def test_signed_zeros_and_flat_regions_bitwise(gpu_lib, port, recon):
             g.advance(dt)
         out = g.download()
     assert np.array_equal(out.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("make", [lambda: W.kelvin_helmholtz(96), lambda: W.mhd_turbulence(10)])
+def test_page_locked_buffers_match_pageable(gpu_lib, precision, make):
+    """A page-locked host array is read and written in place by the
+    conversion kernels; a pageable one is staged in chunks: same bits."""
+    import torch
+    s, P = make()
+    P = W.apply_bc_numpy(s, P)
+    with Solver(s, precision) as g:
+        g.upload(P.copy())
+        dt = g.courant() * s.cfl
+        g.advance(dt)
+        a = g.download()
+        pin = torch.from_numpy(P.copy()).pin_memory()
+        g.upload_ptr(pin.data_ptr())
+        g.advance(dt)
+        out = torch.empty(pin.shape, dtype=torch.float64).pin_memory()
+        g.download_ptr(out.data_ptr())
+        b = out.numpy()
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+        # the drop-in call with the page-locked array, in place
+        assert g.advance_host_ptr(pin.data_ptr(), dt) == 0
+        assert np.array_equal(pin.numpy().view(np.uint64), a.view(np.uint64))
