@@ -160,6 +160,37 @@ int mara_gpu_kernel_times(MaraGpuHandle* h, double ms_total[3], int64_t launches
  * (the reference's default is 1).  MHD and RMHD only. */
 int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs);
 
+/* ---- initial data generated on the device ----------------------------------
+ * MeshOperator::generate (MeshOperator.cpp:168-189) of a built-in initial
+ * data function at every cell centre, guards filled as
+ * BoundaryCondition::applySimple does, then loaded like mara_gpu_upload: the
+ * synthetic problems start without a host array or a host-to-device copy.
+ * Cell centre: lower + dx (i + 0.5) per axis (CartesianMeshGeometry).
+ *   PLANAR_RIEMANN  left where (x - x0) . normal < 0, right elsewhere
+ *                   (shock tubes, Problems.cpp:37-87; oblique interfaces)
+ *   SHEAR_LAYER     left where |y - x0[1]| < radius, right elsewhere; with
+ *                   noise != 0, interior zone (i, j, k) gets velocity2 =
+ *                   (-1 + 2 u) noise, u the top 53 bits of the
+ *                   ((i nj + j) nk + k + 1)-th SplitMix64 output of seed
+ *                   times 2^-53 (Kelvin-Helmholtz)
+ *   CYLINDER        left where sqrt((x - x0)^2 + (y - y0)^2) < radius, right
+ *                   elsewhere (cylindrical blast waves, Problems.cpp:350-375)
+ * States are primitives (nq values). */
+enum { MARA_INIT_PLANAR_RIEMANN = 1, MARA_INIT_SHEAR_LAYER = 2, MARA_INIT_CYLINDER = 3 };
+
+typedef struct MaraInitialData {
+    int kind;
+    double left[8];
+    double right[8];
+    double x0[3];
+    double normal[3];
+    double radius;
+    double noise;
+    unsigned long long seed;
+} MaraInitialData;
+
+int mara_gpu_generate(MaraGpuHandle* h, const MaraInitialData* data);
+
 /* ---- source terms ----------------------------------------------------------
  * MethodOfLinesTVD::setSourceTermsFunction (SolutionSchemes.hpp:36; applied
  * at SolutionSchemes.cpp:219-228): once per RK stage the scheme evaluates the

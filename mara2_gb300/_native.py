@@ -61,6 +61,15 @@ class MaraSourceTermsArgs(C.Structure):
 
 SOURCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(MaraSourceTermsArgs))
 
+MARA_INIT_PLANAR_RIEMANN, MARA_INIT_SHEAR_LAYER, MARA_INIT_CYLINDER = 1, 2, 3
+
+
+class MaraInitialData(C.Structure):
+    """MaraInitialData (include/mara_gpu.h)."""
+    _fields_ = [("kind", C.c_int), ("left", C.c_double * 8), ("right", C.c_double * 8), ("x0", C.c_double * 3),
+                ("normal", C.c_double * 3), ("radius", C.c_double), ("noise", C.c_double),
+                ("seed", C.c_ulonglong)]
+
 SIGNATURES = {
     "mara_gpu_create": (C.c_int, [C.POINTER(MaraGpuConfig), C.POINTER(C.c_void_p)]),
     "mara_gpu_destroy": (C.c_int, [_H]),
@@ -79,6 +88,7 @@ SIGNATURES = {
     "mara_gpu_device_bytes": (C.c_int64, [_H]),
     "mara_gpu_monopole": (C.c_int, [_H, C.c_double, _D]),
     "mara_gpu_num_diagnostics": (C.c_int, [_H]),
+    "mara_gpu_generate": (C.c_int, [_H, C.POINTER(MaraInitialData)]),
     "mara_gpu_set_source_terms": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
     "mara_source_uniform_gravity": (C.c_int, [C.c_void_p, C.POINTER(MaraSourceTermsArgs)]),
     "mara_gpu_volume_diagnostics": (C.c_int, [_H, C.c_void_p, C.POINTER(C.c_int)]),

@@ -113,6 +113,64 @@ __global__ void __launch_bounds__(CONV_BLOCK) k_soa_to_aos(const double* __restr
     for (int e = threadIdx.x; e < nc * nq; e += CONV_BLOCK) aos[b0 * nq + e] = slab[e];
 }
 
+// ---- initial data on the device ----------------------------------------------
+// interior coordinate of full index i along an axis (n interior, g guards),
+// as the boundary condition's guard fill maps it; flip marks a reflection
+__device__ __forceinline__ int bc_interior(int i, int n, int g, int bc, int& flip)
+{
+    const int x = i - g;
+    if (g == 0 || (x >= 0 && x < n)) return x;
+    if (bc == BC_PERIODIC) return x < 0 ? x + n : x - n;
+    if (bc == BC_OUTFLOW) return x < 0 ? 0 : n - 1;
+    flip = 1;
+    return x < 0 ? -1 - x : 2 * n - 1 - x;
+}
+
+struct GenGeom {
+    double lower[3], dx[3];
+};
+
+__global__ void k_generate(double* __restrict__ aos, GridDesc G, GenGeom geo, MaraInitialData d)
+{
+    const long long total = (long long) G.N[0] * G.N[1] * G.N[2];
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;  // AoS order, k fastest
+    if (c >= total) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    int f[3] = {0, 0, 0};
+    const int ii = bc_interior(i, G.n[0], G.g[0], G.bc, f[0]);
+    const int jj = bc_interior(j, G.n[1], G.g[1], G.bc, f[1]);
+    const int kk = bc_interior(k, G.n[2], G.g[2], G.bc, f[2]);
+    const double x = geo.lower[0] + geo.dx[0] * ((double) ii + 0.5);
+    const double y = geo.lower[1] + geo.dx[1] * ((double) jj + 0.5);
+    const double z = geo.lower[2] + geo.dx[2] * ((double) kk + 0.5);
+    bool left;
+    if (d.kind == MARA_INIT_PLANAR_RIEMANN) {
+        left = (x - d.x0[0]) * d.normal[0] + (y - d.x0[1]) * d.normal[1] + (z - d.x0[2]) * d.normal[2] < 0;
+    } else if (d.kind == MARA_INIT_SHEAR_LAYER) {
+        left = fabs(y - d.x0[1]) < d.radius;
+    } else {
+        const double rx = x - d.x0[0], ry = y - d.x0[1];
+        left = sqrt(rx * rx + ry * ry) < d.radius;
+    }
+    double P[8];
+    for (int q = 0; q < G.nq; ++q) P[q] = left ? d.left[q] : d.right[q];
+    if (d.kind == MARA_INIT_SHEAR_LAYER && d.noise != 0.0) {
+        // SplitMix64 (Steele, Lea & Flood 2014), output number m + 1
+        const unsigned long long m = ((unsigned long long) ii * G.n[1] + jj) * G.n[2] + kk;
+        unsigned long long zz = d.seed + (m + 1) * 0x9E3779B97F4A7C15ull;
+        zz = (zz ^ (zz >> 30)) * 0xBF58476D1CE4E5B9ull;
+        zz = (zz ^ (zz >> 27)) * 0x94D049BB133111EBull;
+        zz ^= zz >> 31;
+        const double u = (double) (zz >> 11) * (1.0 / 9007199254740992.0);
+        P[2] = (-1.0 + 2.0 * u) * d.noise;
+    }
+    for (int a = 0; a < 3; ++a)
+        if (f[a]) P[1 + a] *= -1;
+    for (int q = 0; q < G.nq; ++q) aos[c * G.nq + q] = P[q];
+}
+
 void launch_courant_init(DevStatus* st, cudaStream_t s) { k_courant_init<<<1, 1, 0, s>>>(st); }
 void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s)
 {
@@ -511,6 +569,32 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
         h->launches++;
     }
     if (h->mixed) mixed_load_finish(h->mixed, h->st, h->stream);
+    return cuda_status(cudaGetLastError());
+}
+
+int mara_gpu_generate(MaraGpuHandle* h, const MaraInitialData* d)
+{
+    if (!h || !d) return MARA_ERR_ARGUMENT;
+    if (d->kind < MARA_INIT_PLANAR_RIEMANN || d->kind > MARA_INIT_CYLINDER) return MARA_ERR_ARGUMENT;
+    CK(cudaSetDevice(h->cfg.device));
+    GenGeom geo;
+    const int n[3] = {h->cfg.ni, h->cfg.nj, h->cfg.nk};
+    for (int a = 0; a < 3; ++a) {
+        geo.lower[a] = h->cfg.lower[a];
+        geo.dx[a] = (h->cfg.upper[a] - h->cfg.lower[a]) / n[a];
+    }
+    const long long total = h->G.sP;
+    k_generate<<<(unsigned) ((total + 255) / 256), 256, 0, h->stream>>>(h->stage_aos, h->G, geo, *d);
+    k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+    h->launches += 2;
+    if (h->mixed) {
+        mixed_load_begin(h->mixed, h->stream);
+        mixed_load_aos_range(h->mixed, h->stage_aos, 0, total, h->st, h->stream);
+        mixed_load_finish(h->mixed, h->st, h->stream);
+    } else {
+        launch_aos_to_soa_range(h->stage_aos, h->P[h->cur], h->G, 0, total, h->stream);
+    }
+    h->launches++;
     return cuda_status(cudaGetLastError());
 }
 

@@ -139,6 +139,23 @@ class Solver:
     def set_kernel_timing(self, on: bool) -> None:
         self.lib.mara_gpu_set_kernel_timing(self.h, int(on))
 
+    def generate(self, spec: dict) -> None:
+        """MeshOperator::generate of a built-in initial-data function on the
+        device (mara_gpu_generate); spec as workloads.device_initial_data
+        builds it."""
+        d = N.MaraInitialData()
+        d.kind = spec["kind"]
+        for name in ("left", "right"):
+            for q, v in enumerate(spec.get(name, ())):
+                getattr(d, name)[q] = v
+        for name in ("x0", "normal"):
+            for a, v in enumerate(spec.get(name, (0.0, 0.0, 0.0))):
+                getattr(d, name)[a] = v
+        d.radius = spec.get("radius", 0.0)
+        d.noise = spec.get("noise", 0.0)
+        d.seed = spec.get("seed", 0)
+        N.check(self.lib.mara_gpu_generate(self.h, C.byref(d)), "mara_gpu_generate")
+
     def set_source_terms(self, fn=None, gravity=None) -> None:
         """MethodOfLinesTVD::setSourceTermsFunction on the plain path:
         gravity=(g1, g2, g3) installs the library's uniform-gravity source; fn

@@ -90,9 +90,13 @@ def empty_state(s: Scheme) -> np.ndarray:
 # ----------------------------------------------------------------------------
 # workload 1: Sod shock tube (src/Problems.cpp:37-42 states)
 # ----------------------------------------------------------------------------
+def _sod_scheme(n: int, gamma: float = 1.4) -> Scheme:
+    return Scheme(law="hydro", recon="plm", riemann="hlle", bc="outflow", rk_order=2,
+                  shape=(n, 1, 1), gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+
+
 def sod(n: int = 1024, gamma: float = 1.4):
-    s = Scheme(law="hydro", recon="plm", riemann="hlle", bc="outflow", rk_order=2,
-               shape=(n, 1, 1), gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+    s = _sod_scheme(n, gamma)
     P = empty_state(s)
     x, _, _ = cell_centres(s)
     left = x < 0.5
@@ -107,9 +111,13 @@ def sod(n: int = 1024, gamma: float = 1.4):
 KH_SEED = 20261203
 
 
+def _kh_scheme(n: int, riemann: str = "hllc") -> Scheme:
+    return Scheme(law="hydro", recon="plm", riemann=riemann, bc="periodic", rk_order=2,
+                  shape=(n, n, 1), gamma=5.0 / 3, plm_theta=1.5, cfl=0.4, t_final=1.0)
+
+
 def kelvin_helmholtz(n: int = 1024, seed: int = KH_SEED, riemann: str = "hllc"):
-    s = Scheme(law="hydro", recon="plm", riemann=riemann, bc="periodic", rk_order=2,
-               shape=(n, n, 1), gamma=5.0 / 3, plm_theta=1.5, cfl=0.4, t_final=1.0)
+    s = _kh_scheme(n, riemann)
     P = empty_state(s)
     g = s.ng[0]
     _, y, _ = cell_centres(s)
@@ -269,10 +277,14 @@ def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms
 # ----------------------------------------------------------------------------
 # workload 4: relativistic MHD cylindrical blast wave on [-6, 6]^2
 # ----------------------------------------------------------------------------
+def _rmhd_blast_scheme(n: int, pressure_floor: float = -1.0) -> Scheme:
+    return Scheme(law="rmhd", recon="weno5", riemann="hlle", bc="outflow", rk_order=3,
+                  shape=(n, n, 1), lower=(-6.0, -6.0, 0.0), upper=(6.0, 6.0, 1.0), gamma=4.0 / 3,
+                  cfl=0.3, t_final=4.0, pressure_floor=pressure_floor)
+
+
 def rmhd_blast(n: int = 512, pressure_floor: float = -1.0):
-    s = Scheme(law="rmhd", recon="weno5", riemann="hlle", bc="outflow", rk_order=3,
-               shape=(n, n, 1), lower=(-6.0, -6.0, 0.0), upper=(6.0, 6.0, 1.0), gamma=4.0 / 3,
-               cfl=0.3, t_final=4.0, pressure_floor=pressure_floor)
+    s = _rmhd_blast_scheme(n, pressure_floor)
     P = empty_state(s)
     x, y, _ = cell_centres(s)
     r = np.sqrt(x * x + y * y)
@@ -327,10 +339,14 @@ def riemann_stream(count: int = 4096, rate: float = 2000.0, seed: int = RIEMANN_
     return out
 
 
-def riemann_initial(req: RiemannRequest, gamma: float = 5.0 / 3):
+def _riemann_scheme(req: RiemannRequest, gamma: float = 5.0 / 3) -> Scheme:
     shape = (req.n, 1, 1) if req.dims == 1 else (req.n, req.n, 1)
-    s = Scheme(law="hydro", recon="plm", riemann="hllc", bc="outflow", rk_order=2, shape=shape,
-               gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+    return Scheme(law="hydro", recon="plm", riemann="hllc", bc="outflow", rk_order=2, shape=shape,
+                  gamma=gamma, plm_theta=1.5, cfl=0.4, t_final=0.2)
+
+
+def riemann_initial(req: RiemannRequest, gamma: float = 5.0 / 3):
+    s = _riemann_scheme(req, gamma)
     P = empty_state(s)
     x, y, _ = cell_centres(s)
     if req.dims == 1:
@@ -340,3 +356,31 @@ def riemann_initial(req: RiemannRequest, gamma: float = 5.0 / 3):
     for q in range(5):
         P[..., q] = np.where(side, req.left[q], req.right[q])
     return s, apply_bc_numpy(s, P)
+
+
+# ----------------------------------------------------------------------------
+# the same initial data as built-in functions generated on the device
+# (mara_gpu_generate): Scheme plus the MaraInitialData fields
+# ----------------------------------------------------------------------------
+def device_initial_data(name: str, n: int = None, req: RiemannRequest = None):
+    """(Scheme, spec) whose device generation equals the host generator's
+    array bit for bit: "sod", "kh", "rmhd_blast" or "riemann" (req)."""
+    from ._native import MARA_INIT_CYLINDER, MARA_INIT_PLANAR_RIEMANN, MARA_INIT_SHEAR_LAYER
+    if name == "sod":
+        s = _sod_scheme(n)
+        return s, {"kind": MARA_INIT_PLANAR_RIEMANN, "left": (1.0, 0.0, 0.0, 0.0, 1.0),
+                   "right": (0.125, 0.0, 0.0, 0.0, 0.1), "x0": (0.5, 0.5, 0.5), "normal": (1.0, 0.0, 0.0)}
+    if name == "kh":
+        s = _kh_scheme(n)
+        return s, {"kind": MARA_INIT_SHEAR_LAYER, "left": (2.0, 0.5, 0.0, 0.0, 2.5), "right": (1.0, -0.5, 0.0, 0.0, 2.5),
+                   "x0": (0.5, 0.5, 0.5), "radius": 0.25, "noise": 0.01, "seed": KH_SEED}
+    if name == "rmhd_blast":
+        s = _rmhd_blast_scheme(n)
+        return s, {"kind": MARA_INIT_CYLINDER, "left": (0.01, 0.0, 0.0, 0.0, 1.0, 0.1, 0.0, 0.0),
+                   "right": (0.01, 0.0, 0.0, 0.0, 0.01, 0.1, 0.0, 0.0), "x0": (0.0, 0.0, 0.0), "radius": 0.8}
+    if name == "riemann":
+        s = _riemann_scheme(req)
+        nrm = (1.0, 0.0, 0.0) if req.dims == 1 else (math.cos(req.theta), math.sin(req.theta), 0.0)
+        return s, {"kind": MARA_INIT_PLANAR_RIEMANN, "left": req.left, "right": req.right, "x0": (0.5, 0.5, 0.5),
+                   "normal": nrm}
+    raise ValueError(name)
