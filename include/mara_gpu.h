@@ -84,6 +84,10 @@ typedef struct MaraGpuConfig {
     double pressure_floor; /* ConservationLaw::setPressureFloor              */
     int precision;       /* MARA_PRECISION_*                                 */
     int device;          /* CUDA device ordinal                              */
+    double cooling_rate; /* NewtonianMHD::setCoolingRate (ConservationLaws.cpp:
+                            355-358, 489-501): > 0 adds the auxiliary field 8
+                            and the cooling source terms (plain FP64 path;
+                            MHD only, ignored by the other laws); <= 0 none  */
 } MaraGpuConfig;
 
 typedef struct MaraGpuStats {

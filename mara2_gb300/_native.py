@@ -39,6 +39,7 @@ class MaraGpuConfig(C.Structure):
         ("lower", C.c_double * 3), ("upper", C.c_double * 3),
         ("gamma", C.c_double), ("plm_theta", C.c_double), ("shenzha_A", C.c_double),
         ("pressure_floor", C.c_double), ("precision", C.c_int), ("device", C.c_int),
+        ("cooling_rate", C.c_double),
     ]
 
 
@@ -143,4 +144,5 @@ def config_from_scheme(s, precision: str = "fp64", device: int = 0) -> MaraGpuCo
         c.lower[a], c.upper[a] = s.lower[a], s.upper[a]
     c.gamma, c.plm_theta, c.shenzha_A, c.pressure_floor = s.gamma, s.plm_theta, s.shenzha_A, s.pressure_floor
     c.precision, c.device = PRECISION[precision], device
+    c.cooling_rate = s.cooling_rate
     return c

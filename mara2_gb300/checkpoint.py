@@ -45,11 +45,13 @@ MAGIC = b"MARACHK1"
 ALIGN = 64
 
 
-def primitive_names(law: str) -> list:
+def primitive_names(law: str, aux: int = 0) -> list:
     """ConservationLaw::getPrimitiveName (src/ConservationLaws.cpp:310-318,
-    522-533, 861-872)."""
+    522-533, 861-872); NewtonianMHD's auxiliary fields are auxiliary1..."""
     base = ["density", "velocity1", "velocity2", "velocity3", "pressure"]
-    return base if law == "hydro" else base + ["magnetic1", "magnetic2", "magnetic3"]
+    if law == "hydro":
+        return base
+    return base + ["magnetic1", "magnetic2", "magnetic3"] + [f"auxiliary{n + 1}" for n in range(aux)]
 
 
 def point_coordinates(s: Scheme, axis: int) -> np.ndarray:
@@ -109,7 +111,7 @@ class Checkpoint:
 
 def _scheme_dict(s: Scheme) -> dict:
     keys = ("law", "recon", "riemann", "bc", "rk_order", "disable_ct", "weno_is", "shape", "lower", "upper",
-            "gamma", "plm_theta", "shenzha_A", "pressure_floor", "guard", "cfl", "t_final", "steps")
+            "gamma", "plm_theta", "shenzha_A", "pressure_floor", "cooling_rate", "guard", "cfl", "t_final", "steps")
     out = {}
     for k in keys:
         v = getattr(s, k)
@@ -143,7 +145,7 @@ def write_checkpoint(filename: str, s: Scheme, P: np.ndarray, status: dict, user
 
     interior = s.interior()
     full = tuple(s.full_shape[:3])
-    names = primitive_names(s.law)
+    names = primitive_names(s.law, s.aux)
     if P.shape[-1] != len(names):
         raise ValueError("primitive array does not match the conservation law")
     header = {
@@ -207,7 +209,7 @@ def read_checkpoint(filename: str, s: Scheme | None = None) -> Checkpoint:
         return np.frombuffer(data[start:start + 8 * n].tobytes(), dtype="<f8").reshape(entry["shape"]).copy()
 
     s = s or _scheme_from(header["scheme"])
-    names = primitive_names(s.law)
+    names = primitive_names(s.law, s.aux)
     P = np.zeros(s.full_shape)
     interior = s.interior()
     for q, n in enumerate(names):

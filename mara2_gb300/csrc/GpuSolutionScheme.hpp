@@ -39,6 +39,7 @@ struct GpuSchemeOptions
     double gammaLawIndex = 5. / 3;   // ConservationLaw::setGammaLawIndex
     double plmTheta = 1.5;           // MethodOfLinesPlm default
     double pressureFloor = -1.0;     // ConservationLaw::setPressureFloor
+    double coolingRate = -1.0;       // NewtonianMHD::setCoolingRate (> 0: auxiliary field 8)
     int riemannSolver = MARA_RIEMANN_HLLE;
     int wenoSmoothness = MARA_WENO_SHENZHA10;
     double shenZha10A = 50.0;
@@ -170,6 +171,7 @@ private:
         c.plm_theta = opts.plmTheta;
         c.shenzha_A = opts.shenZha10A;
         c.pressure_floor = opts.pressureFloor;
+        c.cooling_rate = opts.coolingRate;
         c.precision = opts.precision;
         c.device = opts.device;
         raise (mara_gpu_create (&c, &handle));

@@ -96,9 +96,11 @@ void launch_volume_diag_plain(int law, const double* P, const GridDesc& G, const
     pp.shenzha_A = ph.shenzha_A;
     pp.pressure_floor = ph.pressure_floor;
     pp.weno_is = ph.weno_is;
+    pp.cooling_rate = ph.cooling_rate;
     switch (law) {
         case LAW_HYDRO: volume_diag_plain<LAW_HYDRO>(P, G, pp, partial, err, out, s); break;
         case LAW_MHD: volume_diag_plain<LAW_MHD>(P, G, pp, partial, err, out, s); break;
+        case LAW_MHD_COOL: volume_diag_plain<LAW_MHD_COOL>(P, G, pp, partial, err, out, s); break;
         default: volume_diag_plain<LAW_RMHD>(P, G, pp, partial, err, out, s); break;
     }
 }

@@ -20,13 +20,15 @@
 
 namespace mara {
 
-constexpr int DIAG_MAX = 17;
+constexpr int DIAG_MAX = 18;
 constexpr int DIAG_BLOCKS = 1024;  // partial sums per reduction
 
-template <int LAW> struct DiagInfo { static constexpr int ND = LAW == LAW_HYDRO ? 5 : 17; };
+template <int LAW> struct DiagInfo {
+    static constexpr int ND = LAW == LAW_HYDRO ? 5 : LAW == LAW_MHD_COOL ? 18 : 17;
+};
 
 // ConservationLaw::makeDiagnostics: NewtonianHydro ConservationLaws.cpp:
-// 321-330, NewtonianMHD :536-574 (no auxiliary fields), RelativisticMHD
+// 321-330, NewtonianMHD :536-574 (with the cooling auxiliary field), RelativisticMHD
 // :874-922
 template <int LAW>
 __device__ __forceinline__ int make_diagnostics(const PhysParams& pp, const double* P, double* D)
@@ -50,7 +52,7 @@ __device__ __forceinline__ int make_diagnostics(const PhysParams& pp, const doub
         const double Ma = sqrt(vv) / ca;
 #pragma unroll
         for (int q = 0; q < 8; ++q) D[q] = U[q];
-        if constexpr (LAW == LAW_MHD) {
+        if constexpr (LAW == LAW_MHD || LAW == LAW_MHD_COOL) {
             D[8] = 0.5 * vv * P[0];
             D[9] = P[4] / (gm - 1.0);
             D[10] = 0.5 * BB;
@@ -74,6 +76,7 @@ __device__ __forceinline__ int make_diagnostics(const PhysParams& pp, const doub
         D[14] = Ma;
         D[15] = s0;
         D[16] = Bv;
+        if constexpr (LAW == LAW_MHD_COOL) D[17] = U[8];  // the auxiliary field
     }
     return ST_OK;
 }

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/mara_gpu.h"
+
 namespace mara {
 
 // Mesh description passed by value to every kernel.  Device arrays are
@@ -46,6 +48,7 @@ struct DevStatus {
 struct PhysParamsH {
     double gamma, plm_theta, shenzha_A, pressure_floor;
     int weno_is;
+    double cooling_rate;
 };
 
 // ---- plain FP64 path (plain_fp64.cu) -----------------------------------------
@@ -70,6 +73,10 @@ void launch_volume_diag_plain(int law, const double* P, const GridDesc& G, const
                               int* err, double* out, cudaStream_t s);
 
 // ---- shared helpers (mara_gpu.cu) --------------------------------------------
+// the law the kernels are instantiated for (LAW_MHD_COOL for NewtonianMHD
+// with a positive cooling rate) and the physics parameters of a configuration
+int kernel_law(const MaraGpuConfig* c);
+void make_phys(const MaraGpuConfig* c, PhysParamsH* pp);
 void launch_courant_init(DevStatus* st, cudaStream_t s);
 void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s);
 void launch_set_dt(DevStatus* st, double dt, cudaStream_t s);

@@ -74,7 +74,7 @@ __global__ void k_run_begin(DevStatus* st, double t)
 // page-locked host memory, reached over the chip-to-chip link) and
 // transposed in shared memory.
 constexpr int CONV_BLOCK = 256;
-constexpr int CONV_MAXQ = 8;
+constexpr int CONV_MAXQ = 10;  // MARA_NUM_FIELDS: the most fields any law carries (NewtonianMHD with cooling: 9)
 
 __device__ __forceinline__ long long soa_index(long long c, const GridDesc& G)
 {
@@ -289,6 +289,9 @@ static int validate(const MaraGpuConfig* c)
         return MARA_ERR_CONFIG;
     if (c->rk_order < 1 || c->rk_order > 3) return MARA_ERR_CONFIG;
     if (c->precision != MARA_PRECISION_FP64 && c->precision != MARA_PRECISION_MIXED) return MARA_ERR_CONFIG;
+    if (c->law == MARA_LAW_MHD && c->cooling_rate > 0.0 && c->precision != MARA_PRECISION_FP64)
+        return MARA_ERR_CONFIG;  // the auxiliary field is on the plain path only
+    static_assert(CONV_MAXQ >= 9, "the layout conversions stage up to 9 fields per cell");
     for (int a = 0; a < 3; ++a) {
         if (n[a] < 1 || c->ng[a] < 0) return MARA_ERR_CONFIG;
         if (n[a] == 1 && c->ng[a] != 0) return MARA_ERR_CONFIG;
@@ -299,6 +302,21 @@ static int validate(const MaraGpuConfig* c)
     if (c->upper[0] <= c->lower[0] || c->upper[1] <= c->lower[1] || c->upper[2] <= c->lower[2])
         return MARA_ERR_CONFIG;
     return MARA_OK;
+}
+
+int mara::kernel_law(const MaraGpuConfig* c)
+{
+    return c->law == MARA_LAW_MHD && c->cooling_rate > 0.0 ? LAW_MHD_COOL : c->law;
+}
+
+void mara::make_phys(const MaraGpuConfig* c, PhysParamsH* pp)
+{
+    pp->gamma = c->gamma;
+    pp->plm_theta = c->plm_theta;
+    pp->shenzha_A = c->shenzha_A;
+    pp->pressure_floor = c->pressure_floor;
+    pp->weno_is = c->weno_is;
+    pp->cooling_rate = c->cooling_rate;
 }
 
 static void make_grid(const MaraGpuConfig* c, GridDesc* G)
@@ -312,7 +330,7 @@ static void make_grid(const MaraGpuConfig* c, GridDesc* G)
         G->N[a] = n[a] + 2 * c->ng[a];
         dx[a] = (c->upper[a] - c->lower[a]) / n[a];
     }
-    G->nq = c->law == MARA_LAW_HYDRO ? 5 : 8;
+    G->nq = c->law == MARA_LAW_HYDRO ? 5 : kernel_law(c) == LAW_MHD_COOL ? 9 : 8;
     G->sP = (long long) G->N[0] * G->N[1] * G->N[2];
     G->sU = (long long) n[0] * n[1] * n[2];
     G->sF = (long long) (G->N[0] + 1) * (G->N[1] + 1) * (G->N[2] + 1);
@@ -352,7 +370,7 @@ static void enqueue_plain_step(MaraGpuHandle* h)
             if (h->G.n[a] <= 1) continue;
             TimedPair tp;
             timed_begin(h, 0, tp);
-            plain_flux(c.law, c.recon, c.riemann, a, h->G, h->pp, h->P[h->cur], h->F[a], h->st, h->stream);
+            plain_flux(kernel_law(&c), c.recon, c.riemann, a, h->G, h->pp, h->P[h->cur], h->F[a], h->st, h->stream);
             timed_end(h, tp);
             h->launches++;
         }
@@ -377,7 +395,7 @@ static void enqueue_plain_step(MaraGpuHandle* h)
         }
         TimedPair tp;
         timed_begin(h, 1, tp);
-        plain_update(c.law, h->G, h->pp, h->P[h->cur], h->P[1 - h->cur], h->U0, h->U, h->F[0], h->F[1], h->F[2],
+        plain_update(kernel_law(&c), h->G, h->pp, h->P[h->cur], h->P[1 - h->cur], h->U0, h->U, h->F[0], h->F[1], h->F[2],
                      b[rk], rk, &h->st->dt, h->st, h->stream, S);
         timed_end(h, tp);
         h->launches++;
@@ -402,7 +420,7 @@ static void enqueue_courant(MaraGpuHandle* h)
     TimedPair tp;
     timed_begin(h, 2, tp);
     if (h->mixed) mixed_enqueue_courant(h->mixed, h->st, h->stream);
-    else plain_courant(h->cfg.law, h->G, h->pp, h->P[h->cur], h->st, h->stream);
+    else plain_courant(kernel_law(&h->cfg), h->G, h->pp, h->P[h->cur], h->st, h->stream);
     timed_end(h, tp);
     h->launches += 2;
 }
@@ -454,11 +472,7 @@ int mara_gpu_create(const MaraGpuConfig* config, MaraGpuHandle** out)
     if (!h) return MARA_ERR_ARGUMENT;
     h->cfg = *config;
     make_grid(config, &h->G);
-    h->pp.gamma = config->gamma;
-    h->pp.plm_theta = config->plm_theta;
-    h->pp.shenzha_A = config->shenzha_A;
-    h->pp.pressure_floor = config->pressure_floor;
-    h->pp.weno_is = config->weno_is;
+    make_phys(config, &h->pp);
     int rc = MARA_OK;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return MARA_ERR_CUDA; }
     if (cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking) != cudaSuccess) rc = MARA_ERR_CUDA;
@@ -576,6 +590,7 @@ int mara_gpu_generate(MaraGpuHandle* h, const MaraInitialData* d)
 {
     if (!h || !d) return MARA_ERR_ARGUMENT;
     if (d->kind < MARA_INIT_PLANAR_RIEMANN || d->kind > MARA_INIT_CYLINDER) return MARA_ERR_ARGUMENT;
+    if (h->G.nq > 8) return MARA_ERR_CONFIG;  // the built-in states hold eight fields
     CK(cudaSetDevice(h->cfg.device));
     GenGeom geo;
     const int n[3] = {h->cfg.ni, h->cfg.nj, h->cfg.nk};
@@ -876,7 +891,7 @@ int mara_gpu_set_source_terms(MaraGpuHandle* h, MaraSourceTermsFn fn, void* user
 int mara_gpu_num_diagnostics(const MaraGpuHandle* h)
 {
     if (!h) return 0;
-    return h->cfg.law == MARA_LAW_HYDRO ? 5 : 17;
+    return h->cfg.law == MARA_LAW_HYDRO ? 5 : kernel_law(&h->cfg) == LAW_MHD_COOL ? 18 : 17;
 }
 
 int mara_gpu_volume_diagnostics(MaraGpuHandle* h, double* D, int* count)
@@ -893,7 +908,7 @@ int mara_gpu_volume_diagnostics(MaraGpuHandle* h, double* D, int* count)
     int* err = (int*) (out + nd);
     CK(cudaMemsetAsync(err, 0, sizeof(int), h->stream));
     if (h->mixed) mixed_volume_diagnostics(h->mixed, partial, err, out, h->stream);
-    else launch_volume_diag_plain(h->cfg.law, h->P[h->cur], h->G, h->pp, partial, err, out, h->stream);
+    else launch_volume_diag_plain(kernel_law(&h->cfg), h->P[h->cur], h->G, h->pp, partial, err, out, h->stream);
     h->launches += 3;
     const int n = mara_gpu_num_diagnostics(h);
     double host[DIAG_MAX + 1];

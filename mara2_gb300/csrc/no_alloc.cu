@@ -109,11 +109,8 @@ extern "C" int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const doubl
         if (G.n[a] > 1) { F[a] = (double*) cur; cur += fbytes; }
 
     PhysParamsH pp;
-    pp.gamma = config->gamma;
-    pp.plm_theta = config->plm_theta;
-    pp.shenzha_A = config->shenzha_A;
-    pp.pressure_floor = config->pressure_floor;
-    pp.weno_is = config->weno_is;
+    make_phys(config, &pp);
+    const int law = kernel_law(config);
 
     // status cleared and dt set; the AoS input is fully transposed into P[0]
     k_noalloc_begin<<<1, 1, 0, s>>>(st, dt);
@@ -127,8 +124,8 @@ extern "C" int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const doubl
     int c = 0;
     for (int rk = 0; rk < config->rk_order; ++rk) {
         for (int a = 0; a < 3; ++a)
-            if (G.n[a] > 1) plain_flux(config->law, config->recon, config->riemann, a, G, pp, P[c], F[a], st, s);
-        plain_update(config->law, G, pp, P[c], P[1 - c], U0, U, F[0], F[1], F[2], b[rk], rk, &st->dt, st, s);
+            if (G.n[a] > 1) plain_flux(law, config->recon, config->riemann, a, G, pp, P[c], F[a], st, s);
+        plain_update(law, G, pp, P[c], P[1 - c], U0, U, F[0], F[1], F[2], b[rk], rk, &st->dt, st, s);
         c = 1 - c;
     }
     launch_soa_to_aos(P[c], P_out, G, s);

@@ -14,7 +14,10 @@
 
 namespace mara {
 
-enum { LAW_HYDRO = 0, LAW_MHD = 1, LAW_RMHD = 2 };
+// LAW_MHD_COOL: NewtonianMHD with a positive cooling rate, which carries one
+// auxiliary field (index 8) fed by the cooling source terms
+// (ConservationLaws.cpp:355-358, 489-501)
+enum { LAW_HYDRO = 0, LAW_MHD = 1, LAW_RMHD = 2, LAW_MHD_COOL = 3 };
 enum { RECON_PCM = 0, RECON_PLM = 1, RECON_WENO5 = 2 };
 enum { RIEMANN_HLLE = 0, RIEMANN_HLLC = 1 };
 enum { BC_PERIODIC = 0, BC_OUTFLOW = 1, BC_REFLECTING = 2 };
@@ -39,6 +42,7 @@ template <int LAW> struct LawInfo;
 template <> struct LawInfo<LAW_HYDRO> { static constexpr int NQ = 5; };
 template <> struct LawInfo<LAW_MHD> { static constexpr int NQ = 8; };
 template <> struct LawInfo<LAW_RMHD> { static constexpr int NQ = 8; };
+template <> struct LawInfo<LAW_MHD_COOL> { static constexpr int NQ = 9; };
 
 // Physics parameters shared by every kernel of a handle.
 struct PhysParams {
@@ -47,6 +51,7 @@ struct PhysParams {
     double shenzha_A;
     double pressure_floor;
     int weno_is;
+    double cooling_rate;  // NewtonianMHD::setCoolingRate (LAW_MHD_COOL)
 };
 
 // A ConservationLaw::State restricted to the law's NQ fields; the reference's
@@ -136,7 +141,8 @@ __device__ __forceinline__ int hydro_cons(const PhysParams& pp, const double* U,
 
 // ---------------------------------------------------------------------------
 // NewtonianMHD::fromPrimitive (ConservationLaws.cpp:416-487)
-__device__ __forceinline__ void mhd_prim(const PhysParams& pp, const double* P, const double* n, StateD<8>& S)
+template <int NQ>
+__device__ __forceinline__ void mhd_prim(const PhysParams& pp, const double* P, const double* n, StateD<NQ>& S)
 {
     const double gm0 = pp.gamma;
     const double gm1 = pp.gamma - 1.0;
@@ -179,8 +185,17 @@ __device__ __forceinline__ void mhd_prim(const PhysParams& pp, const double* P, 
     S.A[5] = vn + sqrt(cS2);
     S.A[6] = vn + sqrt(cn2);
     S.A[7] = vn + sqrt(cF2);
+    // auxiliary fields: carried, no flux, zero eigenvalue (:479-485)
+#pragma unroll
+    for (int q = 8; q < NQ; ++q) {
+        S.P[q] = P[q];
+        S.U[q] = P[q];
+        S.F[q] = 0.0;
+        S.A[q] = 0.0;
+    }
 }
 
+template <int NQ>
 __device__ __forceinline__ void mhd_p2u(const PhysParams& pp, const double* P, double* U)
 {
     const double gm1 = pp.gamma - 1.0;
@@ -194,10 +209,13 @@ __device__ __forceinline__ void mhd_p2u(const PhysParams& pp, const double* P, d
     U[5] = P[5];
     U[6] = P[6];
     U[7] = P[7];
+#pragma unroll
+    for (int q = 8; q < NQ; ++q) U[q] = P[q];
 }
 
 // NewtonianMHD::fromConserved with bad-state detection and the optional
 // pressure floor (ConservationLaws.cpp:370-414)
+template <int NQ>
 __device__ __forceinline__ int mhd_cons(const PhysParams& pp, const double* U, double* P)
 {
     const double gm1 = pp.gamma - 1.0;
@@ -211,6 +229,8 @@ __device__ __forceinline__ int mhd_cons(const PhysParams& pp, const double* U, d
     P[5] = U[5];
     P[6] = U[6];
     P[7] = U[7];
+#pragma unroll
+    for (int q = 8; q < NQ; ++q) P[q] = U[q];
     if (P[4] < 0.0 || P[0] < 0.0 || U[0] < 0.0 || U[4] < 0.0) {
         if (P[4] < 0.0 && pp.pressure_floor > 0.0) {
             P[4] = pp.pressure_floor * P[0];
@@ -596,7 +616,7 @@ __device__ __forceinline__ int law_prim(const PhysParams& pp, const double* P, c
                                         StateD<LawInfo<LAW>::NQ>& S)
 {
     if constexpr (LAW == LAW_HYDRO) { hydro_prim(pp, P, n, S); return ST_OK; }
-    else if constexpr (LAW == LAW_MHD) { mhd_prim(pp, P, n, S); return ST_OK; }
+    else if constexpr (LAW == LAW_MHD || LAW == LAW_MHD_COOL) { mhd_prim<LawInfo<LAW>::NQ>(pp, P, n, S); return ST_OK; }
     else { return rmhd_prim<EIGEN>(pp, P, n, S); }
 }
 
@@ -604,7 +624,7 @@ template <int LAW>
 __device__ __forceinline__ int law_p2u(const PhysParams& pp, const double* P, double* U)
 {
     if constexpr (LAW == LAW_HYDRO) { hydro_p2u(pp, P, U); return ST_OK; }
-    else if constexpr (LAW == LAW_MHD) { mhd_p2u(pp, P, U); return ST_OK; }
+    else if constexpr (LAW == LAW_MHD || LAW == LAW_MHD_COOL) { mhd_p2u<LawInfo<LAW>::NQ>(pp, P, U); return ST_OK; }
     else {
         // FieldOperator::generateConserved calls the full fromPrimitive, whose
         // eigenvalue evaluation can raise "bad eigenvalues"
@@ -621,7 +641,11 @@ template <int LAW>
 __device__ __forceinline__ int law_cons(const PhysParams& pp, const double* U, double* P, int* code)
 {
     if constexpr (LAW == LAW_HYDRO) return hydro_cons(pp, U, P);
-    else if constexpr (LAW == LAW_MHD) { const int e = mhd_cons(pp, U, P); *code = e; return e; }
+    else if constexpr (LAW == LAW_MHD || LAW == LAW_MHD_COOL) {
+        const int e = mhd_cons<LawInfo<LAW>::NQ>(pp, U, P);
+        *code = e;
+        return e;
+    }
     else return rmhd_cons(pp, U, P, code);
 }
 

@@ -102,7 +102,7 @@ struct FluxView {
 template <int NQ>
 __device__ __forceinline__ double face_flux(const FluxView& V, const GridDesc& G, int a, int q, int i, int j, int k)
 {
-    if (NQ == 8 && G.ct && q >= 5) {
+    if ((NQ == 8 || NQ == 9) && G.ct && q >= 5 && q <= 7) {
         const int B0 = 5, B1 = 6, B2 = 7;
         const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
         if (a == 0) {
@@ -207,6 +207,11 @@ __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ 
         const double fzm = fz ? face_flux<NQ>(V, G, 2, q, i, j, k) : 0.0;
         double L = factor / vol * (+fxp * A1000 - fxm * A0000 + fyp * A0101 - fym * A0001
                                    + fzp * A0012 - fzm * A0002);
+        if constexpr (LAW == LAW_MHD_COOL) {
+            // NewtonianMHD::addSourceTerms (ConservationLaws.cpp:489-501)
+            if (q == 4) L -= Pc[4] / (pp.gamma - 1.0) * pp.cooling_rate;
+            if (q == 8) L += Pc[4] / (pp.gamma - 1.0) * pp.cooling_rate;
+        }
         if (S) L += S[q * G.sP + pc];  // the source terms function's array (SolutionSchemes.cpp:219-228)
         Un[q] = Uo[q] * (1 - b) + (Up[q] + dt * L) * b;
         U[q * G.sU + uc] = Un[q];
@@ -310,6 +315,7 @@ static PhysParams to_dev(const PhysParamsH& h)
     p.shenzha_A = h.shenzha_A;
     p.pressure_floor = h.pressure_floor;
     p.weno_is = h.weno_is;
+    p.cooling_rate = h.cooling_rate;
     return p;
 }
 
@@ -355,6 +361,7 @@ void plain_flux(int law, int recon, int riemann, int axis, const GridDesc& G, co
     switch (law) {
         case LAW_HYDRO: flux_dispatch<LAW_HYDRO>(recon, riemann, axis, G, pp, P, F, st, s); break;
         case LAW_MHD: flux_dispatch<LAW_MHD>(recon, riemann, axis, G, pp, P, F, st, s); break;
+        case LAW_MHD_COOL: flux_dispatch<LAW_MHD_COOL>(recon, riemann, axis, G, pp, P, F, st, s); break;
         default: flux_dispatch<LAW_RMHD>(recon, riemann, axis, G, pp, P, F, st, s); break;
     }
 }
@@ -373,6 +380,7 @@ void plain_update(int law, const GridDesc& G, const PhysParamsH& ph, const doubl
     switch (law) {
         case LAW_HYDRO: update_kernel<LAW_HYDRO><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
         case LAW_MHD: update_kernel<LAW_MHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
+        case LAW_MHD_COOL: update_kernel<LAW_MHD_COOL><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
         default: update_kernel<LAW_RMHD><<<grid, block, 0, s>>>(Pin, Pout, U0, U, V, G, pp, b, stage, dt, st, S); break;
     }
 }
@@ -385,6 +393,7 @@ void plain_courant(int law, const GridDesc& G, const PhysParamsH& ph, const doub
     switch (law) {
         case LAW_HYDRO: courant_kernel<LAW_HYDRO><<<grid, block, 0, s>>>(P, G, pp, st); break;
         case LAW_MHD: courant_kernel<LAW_MHD><<<grid, block, 0, s>>>(P, G, pp, st); break;
+        case LAW_MHD_COOL: courant_kernel<LAW_MHD_COOL><<<grid, block, 0, s>>>(P, G, pp, st); break;
         default: courant_kernel<LAW_RMHD><<<grid, block, 0, s>>>(P, G, pp, st); break;
     }
 }

@@ -37,6 +37,7 @@ class Scheme:
     shenzha_A: float = 50.0
     pressure_floor: float = -1.0
     disable_ct: bool = False
+    cooling_rate: float = -1.0        # NewtonianMHD::setCoolingRate: > 0 adds an auxiliary field
     guard: int | None = None          # guard width; default = stencil size
     # driver parameters (not part of advance(), used by run loops)
     cfl: float = 0.4
@@ -51,8 +52,13 @@ class Scheme:
             raise ValueError(f"unknown scheme choice in {self}")
 
     @property
+    def aux(self) -> int:
+        """Auxiliary fields (NewtonianMHD with cooling, ConservationLaws.cpp:355-358)."""
+        return 1 if self.law == "mhd" and self.cooling_rate > 0.0 else 0
+
+    @property
     def nq(self) -> int:
-        return NFIELDS[self.law]
+        return NFIELDS[self.law] + self.aux
 
     @property
     def stencil(self) -> int:

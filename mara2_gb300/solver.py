@@ -14,15 +14,16 @@ from . import _native as N
 from .scheme import Scheme
 
 
-def diagnostic_names(law: str) -> list:
+def diagnostic_names(law: str, aux: int = 0) -> list:
     """ConservationLaw::getDiagnosticNames (src/ConservationLaws.cpp:332-341,
-    576-601, 924-945)."""
+    576-601, 924-945); aux auxiliary fields of NewtonianMHD add
+    auxiliary1..."""
     base = ["mass", "momentum1", "momentum2", "momentum3", "total_energy"]
     if law == "hydro":
         return base
     return base + ["magnetic_flux1", "magnetic_flux2", "magnetic_flux3", "kinetic_energy", "internal_energy",
                    "magnetic_energy", "sound_speed", "alfven_speed", "sonic_mach_number", "alfven_mach_number",
-                   "specific_entropy", "cross_helicity"]
+                   "specific_entropy", "cross_helicity"] + [f"auxiliary{n + 1}" for n in range(aux)]
 
 
 class Solver:
@@ -185,7 +186,7 @@ class Solver:
         cnt = C.c_int(0)
         N.check(self.lib.mara_gpu_volume_diagnostics(self.h, D.ctypes.data, C.byref(cnt)),
                 "mara_gpu_volume_diagnostics")
-        return dict(zip(diagnostic_names(self.scheme.law), D.tolist()))
+        return dict(zip(diagnostic_names(self.scheme.law, self.scheme.aux), D.tolist()))
 
     def field_diagnostics(self, mesh_spacing: float = 1.0) -> np.ndarray:
         """[monopole, current1, current2, current3] at every cell of the array

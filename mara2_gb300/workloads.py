@@ -277,6 +277,17 @@ def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms
 # ----------------------------------------------------------------------------
 # workload 4: relativistic MHD cylindrical blast wave on [-6, 6]^2
 # ----------------------------------------------------------------------------
+def with_cooling(s: Scheme, P: np.ndarray, rate: float, aux: float = 0.0):
+    """NewtonianMHD with cooling (setCoolingRate, ConservationLaws.cpp:355-358):
+    the scheme with the rate and the state with the auxiliary field (index 8)
+    set to aux."""
+    if s.law != "mhd" or not rate > 0.0:
+        raise ValueError("cooling needs the MHD law and a positive rate")
+    s2 = s.with_(cooling_rate=rate)
+    P2 = np.concatenate([P[..., :8], np.full(P.shape[:3] + (1,), float(aux))], axis=-1)
+    return s2, P2
+
+
 def _rmhd_blast_scheme(n: int, pressure_floor: float = -1.0) -> Scheme:
     return Scheme(law="rmhd", recon="weno5", riemann="hlle", bc="outflow", rk_order=3,
                   shape=(n, n, 1), lower=(-6.0, -6.0, 0.0), upper=(6.0, 6.0, 1.0), gamma=4.0 / 3,

@@ -81,11 +81,13 @@ int mo_num_fields(const mo_config* c)
 {
     switch (c->law) {
         case MO_LAW_HYDRO: return 5;
-        case MO_LAW_MHD: return 8;
+        case MO_LAW_MHD: return c->cooling_rate > 0.0 ? 9 : 8;  /* numAuxiliary, ConservationLaws.cpp:355-358 */
         case MO_LAW_RMHD: return 8;
         default: return 0;
     }
 }
+
+static int mhd_aux(const mo_config* c) { return c->law == MO_LAW_MHD && c->cooling_rate > 0.0; }
 
 int mo_stencil_size(const mo_config* c)
 {
@@ -188,7 +190,7 @@ static int hydro_cons(double gamma, const double* U, double* P)
 /* NewtonianMHD::fromPrimitive (ConservationLaws.cpp:416-487), Jameson's     */
 /* fast / Alfven / slow speeds                                               */
 /* ------------------------------------------------------------------------ */
-static int mhd_prim(double gamma, const double* P, const double* n, mstate* S)
+static int mhd_prim(double gamma, int naux, const double* P, const double* n, mstate* S)
 {
     const double gm0 = gamma;
     const double gm1 = gamma - 1.0;
@@ -234,18 +236,27 @@ static int mhd_prim(double gamma, const double* P, const double* n, mstate* S)
         S->A[6] = vn + sqrt(cn2);
         S->A[7] = vn + sqrt(cF2);
     }
+    /* auxiliary fields: carried, no flux, zero eigenvalue (:479-485) */
+    for (int q = 8; q < 8 + naux; ++q) {
+        S->P[q] = P[q];
+        S->U[q] = P[q];
+        S->F[q] = 0.0;
+        S->A[q] = 0.0;
+    }
+    S->nf = 8 + naux;
     return MO_OK;
 }
 
 /* NewtonianMHD::fromConserved incl. bad-state detection and pressure floor
  * (ConservationLaws.cpp:370-414).  Returns MO_ERR_INVERSION_FAILURE for a
  * StateFailure. */
-static int mhd_cons(double gamma, double pfloor, const double* U, double* P, int* health)
+static int mhd_cons(double gamma, double pfloor, int naux, const double* U, double* P, int* health)
 {
     const double gm1 = gamma - 1.0;
     const double pp = U[1] * U[1] + U[2] * U[2] + U[3] * U[3];
     const double BB = U[5] * U[5] + U[6] * U[6] + U[7] * U[7];
-    double Q[8];
+    double Q[9];
+    const int nf = 8 + naux;
     Q[0] = U[0];
     Q[4] = (U[4] - 0.5 * pp / U[0] - 0.5 * BB) * gm1;
     Q[1] = U[1] / U[0];
@@ -254,17 +265,18 @@ static int mhd_cons(double gamma, double pfloor, const double* U, double* P, int
     Q[5] = U[5];
     Q[6] = U[6];
     Q[7] = U[7];
+    for (int q = 8; q < nf; ++q) Q[q] = U[q];
     *health = 0;
     if (Q[4] < 0.0 || Q[0] < 0.0 || U[0] < 0.0 || U[4] < 0.0) {
         if (Q[4] < 0.0 && pfloor > 0.0) {
             Q[4] = pfloor * Q[0];
             *health = 1;
         } else {
-            for (int q = 0; q < 8; ++q) P[q] = Q[q];
+            for (int q = 0; q < nf; ++q) P[q] = Q[q];
             return MO_ERR_INVERSION_FAILURE;
         }
     }
-    for (int q = 0; q < 8; ++q) P[q] = Q[q];
+    for (int q = 0; q < nf; ++q) P[q] = Q[q];
     return MO_OK;
 }
 
@@ -662,7 +674,7 @@ static int from_prim(const mo_config* c, const double* P, const double* n, mstat
 {
     switch (c->law) {
         case MO_LAW_HYDRO: return hydro_prim(c->gamma, P, n, S);
-        case MO_LAW_MHD: return mhd_prim(c->gamma, P, n, S);
+        case MO_LAW_MHD: return mhd_prim(c->gamma, mhd_aux(c), P, n, S);
         case MO_LAW_RMHD: return rmhd_prim(c->gamma, P, n, S);
         default: return MO_ERR_CONFIG;
     }
@@ -673,7 +685,7 @@ static int from_cons(const mo_config* c, const double* U, double* P, int* health
     *health = 0;
     switch (c->law) {
         case MO_LAW_HYDRO: return hydro_cons(c->gamma, U, P);
-        case MO_LAW_MHD: return mhd_cons(c->gamma, c->pressure_floor, U, P, health);
+        case MO_LAW_MHD: return mhd_cons(c->gamma, c->pressure_floor, mhd_aux(c), U, P, health);
         case MO_LAW_RMHD: return rmhd_cons(c->gamma, c->pressure_floor, U, P, health);
         default: return MO_ERR_CONFIG;
     }
@@ -1292,6 +1304,16 @@ int mo_advance(const mo_config* c, double* P, double t0, double dt, mo_failure* 
                                 - F[fidx(&g, i, j, k, q, 2)] * A0002);
         }
 
+        /* ConservationLaw::addSourceTerms (SolutionSchemes.cpp:201):
+         * NewtonianMHD cooling (ConservationLaws.cpp:489-501) over every cell */
+        if (mhd_aux(c)) {
+            const double gm1 = c->gamma - 1.0;
+            for (long n = 0; n < ncell; ++n) {
+                const double p = P[n * g.nq + 4];
+                L[n * g.nq + 4] -= p / gm1 * c->cooling_rate;
+                L[n * g.nq + 8] += p / gm1 * c->cooling_rate;
+            }
+        }
         if (g_src_fn) add_source_terms(c, &g, P, L);
 
         /* RK combine over every element (SolutionSchemes.cpp:232-235) */
@@ -1389,7 +1411,7 @@ int mo_num_diagnostics(const mo_config* c)
 {
     switch (c->law) {
         case MO_LAW_HYDRO: return 5;
-        case MO_LAW_MHD: return 17;
+        case MO_LAW_MHD: return 17 + mhd_aux(c);
         case MO_LAW_RMHD: return 17;
         default: return 0;
     }
@@ -1441,6 +1463,7 @@ static int make_diagnostics(const mo_config* c, const double* P, double* D)
     D[14] = Ma;
     D[15] = s0;
     D[16] = Bv;
+    if (mhd_aux(c)) D[17] = S.U[8];
     return MO_OK;
 }
 
@@ -1463,7 +1486,7 @@ int mo_volume_diagnostics(const mo_config* c, const double* P, double* D, double
     for (int i = c->ng[0]; i < c->ng[0] + c->ni; ++i)
         for (int j = c->ng[1]; j < c->ng[1] + c->nj; ++j)
             for (int k = c->ng[2]; k < c->ng[2] + c->nk; ++k) {
-                double d[17];
+                double d[18];
                 err = make_diagnostics(c, P + cidx(&g, i, j, k), d);
                 if (err) return err;
                 for (int n = 0; n < nd; ++n) {

@@ -67,6 +67,8 @@ typedef struct mo_config {
     double plm_theta;
     double shenzha_A;
     double pressure_floor;
+    double cooling_rate; /* NewtonianMHD::setCoolingRate: > 0 adds the     */
+                         /* auxiliary field 8 and the cooling source terms  */
 } mo_config;
 
 typedef struct mo_failure {

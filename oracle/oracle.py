@@ -49,7 +49,7 @@ class Config(C.Structure):
         ("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("ng", C.c_int * 3),
         ("lower", C.c_double * 3), ("upper", C.c_double * 3),
         ("gamma", C.c_double), ("plm_theta", C.c_double), ("shenzha_A", C.c_double),
-        ("pressure_floor", C.c_double),
+        ("pressure_floor", C.c_double), ("cooling_rate", C.c_double),
     ]
 
 
@@ -60,7 +60,7 @@ class Failure(C.Structure):
 def make_config(law="hydro", recon="plm", riemann="hlle", bc="outflow", rk_order=2,
                 shape=(64, 1, 1), lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0), gamma=5.0 / 3,
                 plm_theta=1.5, weno_is="shenzha10", shenzha_A=50.0, pressure_floor=-1.0,
-                disable_ct=False, ng=None) -> Config:
+                disable_ct=False, ng=None, cooling_rate=-1.0) -> Config:
     c = Config()
     c.law, c.recon, c.riemann, c.bc = LAW[law], RECON[recon], RIEMANN[riemann], BC[bc]
     c.rk_order, c.disable_ct, c.weno_is = rk_order, int(disable_ct), WENO_IS[weno_is]
@@ -70,11 +70,12 @@ def make_config(law="hydro", recon="plm", riemann="hlle", bc="outflow", rk_order
         c.ng[a] = g if shape[a] > 1 else 0
         c.lower[a], c.upper[a] = lower[a], upper[a]
     c.gamma, c.plm_theta, c.shenzha_A, c.pressure_floor = gamma, plm_theta, shenzha_A, pressure_floor
+    c.cooling_rate = cooling_rate
     return c
 
 
 def config_nq(c: Config) -> int:
-    return (5, 8, 8)[c.law]
+    return (5, 9 if c.cooling_rate > 0.0 else 8, 8)[c.law]
 
 
 def full_shape(c: Config) -> tuple:
@@ -233,7 +234,7 @@ class Oracle:
         """(status, D, Dabs): FieldOperator::volumeIntegratedDiagnostics over
         the interior of P, and the sum of the terms' magnitudes (zeros from the
         reference build, which does not form it)."""
-        nd = 5 if c.law == LAW["hydro"] else 17
+        nd = 5 if c.law == LAW["hydro"] else 18 if (c.law == LAW["mhd"] and c.cooling_rate > 0.0) else 17
         D, Dabs = np.zeros(nd), np.zeros(nd)
         status = self._f("volume_diagnostics")(C.byref(c), _ptr(np.ascontiguousarray(P, dtype=float)), _ptr(D),
                                                 _ptr(Dabs))

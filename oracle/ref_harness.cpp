@@ -120,6 +120,7 @@ static Setup make_setup (const mo_config* c)
     }
     s.cl->setGammaLawIndex (c->gamma);
     s.cl->setPressureFloor (c->pressure_floor);
+    s.cl->setCoolingRate (c->cooling_rate);
     s.nq = s.cl->getNumConserved();
 
     s.fo = std::make_shared<FieldOperator>();

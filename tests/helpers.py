@@ -11,7 +11,7 @@ def oracle_config(s):
                          shape=s.shape, lower=s.lower, upper=s.upper, gamma=s.gamma,
                          plm_theta=s.plm_theta, weno_is=s.weno_is, shenzha_A=s.shenzha_A,
                          pressure_floor=s.pressure_floor, disable_ct=s.disable_ct,
-                         ng=max(s.ng))
+                         ng=max(s.ng), cooling_rate=s.cooling_rate)
 
 
 def rel_l1(a, b, axis_q=None):

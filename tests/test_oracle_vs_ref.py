@@ -201,3 +201,24 @@ def test_source_terms_bitwise(port, ref, make, src):
         ref.set_source_terms(None)
     assert np.array_equal(_bits(A), _bits(B))
     assert not np.array_equal(_bits(A), _bits(P))
+
+
+@pytest.mark.parametrize("make,kw", [(lambda: W.mhd_turbulence(6), {}),
+                                     (lambda: W.mhd_turbulence(6), dict(disable_ct=True, rk_order=3))])
+def test_cooling_bitwise(port, ref, make, kw):
+    """NewtonianMHD with a cooling rate: the auxiliary field 8 and
+    addSourceTerms (ConservationLaws.cpp:355-358, 479-501), advances and the
+    18 volume diagnostics."""
+    s, P = make()
+    s, P = W.with_cooling(s.with_(**kw), P, 0.4, aux=0.02)
+    c = oracle_config(s)
+    assert O.config_nq(c) == 9
+    A, B = P.copy(), P.copy()
+    for _ in range(3):
+        _, dt = port.courant(c, A)
+        assert port.advance(c, A, s.cfl * dt)[0] == 0
+        assert ref.advance(c, B, s.cfl * dt)[0] == 0
+    assert np.array_equal(_bits(A), _bits(B))
+    assert A[..., 8].mean() > 0.02                      # energy moved into the auxiliary field
+    a, b = port.volume_diagnostics(c, A), ref.volume_diagnostics(c, A)
+    assert len(a[1]) == 18 and np.array_equal(_bits(a[1]), _bits(b[1]))
