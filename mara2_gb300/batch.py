@@ -200,7 +200,9 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bo
                 queue.popleft()
                 inflight[slot] = (r, s, time.perf_counter() - t0)
             if inflight:
-                b.step(steps_per_poll)
+                # while requests wait to arrive or to be admitted, poll often;
+                # afterwards only retirement waits on a poll
+                b.step(steps_per_poll if (queue or pending) else 4 * steps_per_poll)
                 for slot in b.poll():
                     r, s, t_admit = inflight.pop(slot)
                     out, t, nsteps = b.retire(slot, s.full_shape)

@@ -40,7 +40,7 @@ struct SlotHost {
 };
 
 __global__ void k_slot_init(HGrid* grids, int* rot, double* t, double* dt, double* tfin, double* cflp, int* done,
-                            long long* steps, int slot, HGrid g, double t_final, double cfl)
+                            long long* steps, int* pend, int slot, HGrid g, double t_final, double cfl)
 {
     grids[slot] = g;
     rot[slot] = 0;
@@ -50,38 +50,35 @@ __global__ void k_slot_init(HGrid* grids, int* rot, double* t, double* dt, doubl
     cflp[slot] = cfl;
     done[slot] = 0;
     steps[slot] = 0;
+    pend[slot] = 0;
 }
 
 __global__ void k_slot_clear(int* done, int slot) { done[slot] = 1; }
 
-// per-grid dt of the drivers: dt = min(cfl * courant, t_final - t); a grid
-// whose t has reached t_final stops (MeshData left as after its last step)
-__global__ void k_batch_dt(int n, const unsigned long long* cflbits, const double* cflp, const double* t,
-                           const double* tfin, double* dt, int* done)
+// Start of a batch step, one thread per slot: the previous step's clock
+// advance (t += dt, the step count, the RK1 buffer swap), then the drivers'
+// dt = min(cfl * courant, t_final - t) (src/Problems.cpp:181-186) from the
+// Courant step the previous step's last stage (or the load) reduced, and the
+// reduction slot reset for this step's last stage.  A grid whose t has
+// reached t_final stops (done = 2) with its state as after its last step.
+__global__ void k_batch_begin(int n, unsigned long long* cflbits, const double* cflp, double* t, const double* tfin,
+                              double* dt, int* done, long long* steps, int* rot, int* pend, int flip)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n || done[s]) return;
+    if (pend[s]) {
+        t[s] += dt[s];
+        steps[s] += 1;
+        if (flip) rot[s] ^= 1;
+        pend[s] = 0;
+    }
     if (!(t[s] < tfin[s])) { done[s] = 2; return; }   // 2: finished (1: empty slot)
     const double courant = __longlong_as_double((long long) cflbits[s]);
     double d = cflp[s] * courant;
     const double d2 = tfin[s] - t[s];
     dt[s] = d < d2 ? d : d2;
-}
-
-__global__ void k_batch_cfl_reset(int n, const int* done, unsigned long long* cflbits)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < n && !done[s]) cflbits[s] = (unsigned long long) __double_as_longlong(DBL_MAX);
-}
-
-__global__ void k_batch_time(int n, const int* done, const double* dt, double* t, long long* steps, int* rot,
-                             int flip)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || done[s]) return;
-    t[s] += dt[s];
-    steps[s] += 1;
-    if (flip) rot[s] ^= 1;
+    cflbits[s] = (unsigned long long) __double_as_longlong(DBL_MAX);
+    pend[s] = 1;
 }
 
 __global__ void k_set_int(int* p, int v) { *p = v; }
@@ -150,6 +147,7 @@ struct MaraBatch {
     int* rot = nullptr;
     double *t = nullptr, *dt = nullptr, *tfin = nullptr, *cflp = nullptr;
     int* done = nullptr;
+    int* pend = nullptr;    // a step was taken whose clock advance the next step start applies
     long long* steps = nullptr;
     unsigned long long* cflbits = nullptr;
     TileRef* tiles[2] = {nullptr, nullptr};
@@ -170,7 +168,10 @@ struct MaraBatch {
     int64_t launches = 0;
     int tile1 = 256, tile2 = 2;
     int ctas[2] = {0, 0};
-    cudaGraphExec_t graph = nullptr;
+    int count[2] = {0, 0};  // tiles in each list (host copy)
+    // one captured step per combination of non-empty tile lists (bit 0: 1-D,
+    // bit 1: 2-D), so that a step launches only the lists that hold tiles
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 typedef void (*TileKernel)(const HGrid*, const TileRef*, const int*, const int*, const double*, int, const int*, int,
@@ -221,17 +222,20 @@ static int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MARA_OK : MARA_ERR
 
 static const float B_TABLE[3][3] = {{1.f, 0.f, 0.f}, {1.f, 0.5f, 0.f}, {1.f, 0.25f, 2.f / 3.f}};
 
-static void enqueue_batch_step(MaraBatch* b)
+static int list_mask(const MaraBatch* b) { return (b->count[0] > 0 ? 1 : 0) | (b->count[1] > 0 ? 2 : 0); }
+
+static void enqueue_batch_step(MaraBatch* b, int mask)
 {
     const int n = b->nslots, nb = (n + 255) / 256;
     const cudaStream_t s = b->stream;
-    k_batch_dt<<<nb, 256, 0, s>>>(n, b->cflbits, b->cflp, b->t, b->tfin, b->dt, b->done);
     const int order = b->cfg.rk_order;
+    k_batch_begin<<<nb, 256, 0, s>>>(n, b->cflbits, b->cflp, b->t, b->tfin, b->dt, b->done, b->steps, b->rot, b->pend,
+                                     order == 1 ? 1 : 0);
     for (int rk = 0; rk < order; ++rk) {
         const int last = rk == order - 1;
-        if (last) k_batch_cfl_reset<<<nb, 256, 0, s>>>(n, b->done, b->cflbits);
         const float bb = B_TABLE[order - 1][rk];
         for (int d = 0; d < 2; ++d) {
+            if (!(mask & (1 << d))) continue;
             int tx, ty, nt;
             tile_dims(b, d + 1, &tx, &ty, &nt);
             TileKernel k = kernel_for(b, d + 1);
@@ -239,10 +243,13 @@ static void enqueue_batch_step(MaraBatch* b)
                                         1.f - bb, last, b->cflbits, 1);
         }
     }
-    k_batch_time<<<nb, 256, 0, s>>>(n, b->done, b->dt, b->t, b->steps, b->rot, order == 1 ? 1 : 0);
 }
 
-static int launches_per_step(const MaraBatch* b) { return 2 + b->cfg.rk_order * 2 + 1; }
+static int launches_per_step(const MaraBatch* b)
+{
+    const int mask = list_mask(b);
+    return 1 + b->cfg.rk_order * ((mask & 1) + ((mask >> 1) & 1));
+}
 
 static int upload_tiles(MaraBatch* b)
 {
@@ -266,6 +273,7 @@ static int upload_tiles(MaraBatch* b)
         if (count[d]) BK(cudaMemcpyAsync(b->tiles[d], b->tiles_host[d][which], sizeof(TileRef) * count[d],
                                          cudaMemcpyHostToDevice, b->stream));
         k_set_int<<<1, 1, 0, b->stream>>>(b->ntiles + d, count[d]);
+        b->count[d] = count[d];
     }
     BK(cudaEventRecord(b->tiles_ev[which], b->stream));
     b->tiles_buf = which;
@@ -308,6 +316,7 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
     A((void**) &b->tfin, sizeof(double) * n);
     A((void**) &b->cflp, sizeof(double) * n);
     A((void**) &b->done, sizeof(int) * n);
+    A((void**) &b->pend, sizeof(int) * n);
     A((void**) &b->steps, sizeof(long long) * n);
     A((void**) &b->cflbits, sizeof(unsigned long long) * n);
     A((void**) &b->ntiles, sizeof(int) * 2);
@@ -331,6 +340,7 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
         cudaMemcpy(b->done, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
         cudaMemset(b->ntiles, 0, sizeof(int) * 2);
         cudaMemset(b->rot, 0, sizeof(int) * n);
+        cudaMemset(b->pend, 0, sizeof(int) * n);
         for (int d = 0; d < 2; ++d) {
             int tx, ty, nt, per = 0;
             tile_dims(b, d + 1, &tx, &ty, &nt);
@@ -349,7 +359,8 @@ int mara_batch_destroy(MaraBatch* b)
     if (!b) return MARA_OK;
     cudaSetDevice(b->cfg.device);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& g : b->graph) if (g) cudaGraphExecDestroy(g);
+    cudaFree(b->pend);
     for (auto& h : b->slots)
         for (int k = 0; k < 6; ++k)
             if (h.bufs[k]) cudaFree(h.bufs[k]);
@@ -419,8 +430,8 @@ int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* c, const double* P_aos, 
     g.lmin = (float) std::min(dx, std::min(dy, dz));
 
     BK(cudaMemcpyAsync(b->staging, P_aos, sizeof(double) * (size_t) N0 * N1 * 5, cudaMemcpyHostToDevice, b->stream));
-    k_slot_init<<<1, 1, 0, b->stream>>>(b->grids, b->rot, b->t, b->dt, b->tfin, b->cflp, b->done, b->steps, sl, g,
-                                        t_final, cfl);
+    k_slot_init<<<1, 1, 0, b->stream>>>(b->grids, b->rot, b->t, b->dt, b->tfin, b->cflp, b->done, b->steps, b->pend,
+                                        sl, g, t_final, cfl);
     k_set_u64<<<1, 1, 0, b->stream>>>(b->cflbits + sl, ~0ull);
     dim3 grid((c->ni + 255) / 256, c->nj);
     k_batch_load<<<grid, 256, 0, b->stream>>>(b->staging, g, h.g0, h.g1, N0, N1, 1.0 / (c->gamma - 1.0),
@@ -441,16 +452,17 @@ int mara_batch_step(MaraBatch* b, int steps)
         if (rc) return rc;
         b->launches += 2;
     }
-    if (!b->graph) {
+    const int mask = list_mask(b);
+    if (!b->graph[mask]) {
         cudaGraph_t g;
         BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_batch_step(b);
+        enqueue_batch_step(b, mask);
         BK(cudaStreamEndCapture(b->stream, &g));
-        const cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+        const cudaError_t e = cudaGraphInstantiate(&b->graph[mask], g, 0);
         cudaGraphDestroy(g);
         BK(e);
     }
-    for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph, b->stream));
+    for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph[mask], b->stream));
     b->step_count += steps;
     b->launches += (int64_t) steps * launches_per_step(b);
     return MARA_OK;
