@@ -1,0 +1,213 @@
+// hydro_cluster.cuh -- many driver-loop steps of a small 1-D hydro grid in one
+// launch, on one thread-block cluster (mixed precision, the arithmetic of
+// the fused stage kernel in hydro_tile.cuh).
+//
+// A 1-D grid of up to CLUSTER1D_MAX_CTAS x 1024 zones stays in the shared
+// memory of a cluster of C CTAs for the whole launch: CTA r holds zones
+// [r m, (r + 1) m) of the FP32-pair state and of U0.  Per RK stage each CTA
+// converts its zones to primitives, the cluster synchronises, each CTA reads
+// its stencil-wide halo from its neighbours' shared memory (distributed
+// shared memory) or from the boundary image of the grid's edge, computes its
+// faces and updates its zones in place.  The Courant step of the new state is
+// reduced across the cluster through shared memory too, so the next step's
+// dt = min(cfl x courant, t_final - t) (src/Problems.cpp:181-186) is known to
+// every CTA without leaving the SMs.  Per step this replaces three kernel
+// launches and the passes over the state in HBM with two cluster barriers
+// per stage: a small grid is latency-bound, not bandwidth-bound.
+#pragma once
+
+#include <cooperative_groups.h>
+#include <cfloat>
+
+#include "hydro_tile.cuh"
+#include "internal.h"
+
+namespace mara {
+
+constexpr int CLUSTER1D_MAX_CTAS = 8;  // portable cluster size
+constexpr int CLUSTER1D_MAX_ZONES_PER_CTA = 1024;
+
+// dynamic shared memory of a CTA holding m zones with a halo of G: U hi/lo
+// and U0 hi/lo (5 fields each), primitives with halo, face fluxes, the
+// CTA's Courant slot
+__host__ __device__ constexpr size_t cluster1d_smem_bytes(int m, int G)
+{
+    return sizeof(float) * (4 * 5 * (size_t) m + 5 * (size_t) (m + 2 * G) + 5 * (size_t) (m + 1) + 4);
+}
+
+// Driver-loop steps (at most nsteps, stopping at t_final when t_final >= 0)
+// of the grid g, whose state is buffer s of its rotation; the state is
+// written back to buffer s.  st holds the clock (t, steps, dt, done) as the
+// graph-replayed steps keep it; *cfl_bits holds the Courant step of the state
+// (bits of a positive double) on entry and on exit.
+template <int RECON, int RIEMANN>
+__global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(HGrid g, int s, int order, int nsteps, double cfl,
+                                                               double t_final, DevStatus* __restrict__ st,
+                                                               unsigned long long* __restrict__ cfl_bits)
+{
+    namespace cg = cooperative_groups;
+    constexpr int G = HaloOf<RECON>::G;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int) cluster.num_blocks();
+    const int r = (int) cluster.block_rank();
+    const int n = g.n0;
+    const int m = (n + C - 1) / C;                 // zones per CTA
+    const int z0 = r * m;
+    const int mine = max(0, min(m, n - z0));       // zones this CTA owns
+
+    extern __shared__ float smem[];
+    float* Uh = smem;                              // [5][m]
+    float* Ul = Uh + 5 * m;
+    float* U0h = Ul + 5 * m;
+    float* U0l = U0h + 5 * m;
+    float* Ps = U0l + 5 * m;                       // [5][m + 2G], zone z at z + G
+    float* Fx = Ps + 5 * (m + 2 * G);              // [5][m + 1]
+    float* red = Fx + 5 * (m + 1);                 // this CTA's Courant slot
+    const int W = m + 2 * G;
+    __shared__ float wmin[32];
+    float* __restrict__ gh = s == 0 ? g.Uh[0] : s == 1 ? g.Uh[1] : g.Uh[2];
+    float* __restrict__ gl = s == 0 ? g.Ul[0] : s == 1 ? g.Ul[1] : g.Ul[2];
+
+    for (int i = threadIdx.x; i < mine; i += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            Uh[q * m + i] = gh[q * g.sU + z0 + i];
+            Ul[q * m + i] = gl[q * g.sU + z0 + i];
+        }
+    }
+    // every CTA follows the same clock: the same doubles from the same inputs
+    double t = st->t;
+    long long steps = st->steps;
+    int done = st->done;
+    double dt = st->dt;
+    unsigned long long bits = *cfl_bits;
+    unsigned long long used = st->dt_bits;       // the Courant step the last dt came from
+    cluster.sync();
+
+    for (int step = 0; step < nsteps && !done; ++step) {
+        // the step start of the fused path (k_fused_run_begin)
+        used = bits;
+        dt = cfl * __longlong_as_double((long long) bits);
+        if (t_final >= 0.0) {
+            if (!(t < t_final)) { done = 1; break; }
+            const double dt2 = t_final - t;
+            dt = dt < dt2 ? dt : dt2;
+        }
+        const float dtf = (float) dt;
+        float zdt = 3.0e38f;
+        for (int rk = 0; rk < order; ++rk) {
+            const int last = rk == order - 1;
+            const float b = order == 1 ? 1.f : order == 2 ? (rk == 0 ? 1.f : 0.5f)
+                                                          : (rk == 0 ? 1.f : rk == 1 ? 0.25f : 2.f / 3.f);
+            const float omb = 1.f - b;
+            // 1. primitives of the owned zones (from the high words)
+            for (int i = threadIdx.x; i < mine; i += blockDim.x) {
+                float U[5], P[5];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) U[q] = Uh[q * m + i];
+                hydro_cons_f(g.gamma, U, P);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) Ps[q * W + G + i] = P[q];
+            }
+            cluster.sync();
+            // 2. the halo: 2G zones from the neighbours' shared memory, or the
+            //    boundary image of the grid's edge (momentum negated across a
+            //    reflecting boundary)
+            if (threadIdx.x < 2 * G) {
+                const int k = threadIdx.x;
+                const int local = k < G ? k - G : mine + (k - G);  // zone index relative to z0
+                int flip = 0;
+                const int z = bc_image(z0 + local, n, g.bc, flip);
+                const int owner = z / m, at = z - owner * m;
+                const float* src = cluster.map_shared_rank(Ps, owner);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    float v = src[q * W + G + at];
+                    if (flip && q == 1) v = -v;
+                    Ps[q * W + G + local] = v;
+                }
+            }
+            __syncthreads();
+            // 3. faces: face f sits left of owned zone f, f = 0..mine
+            for (int f = threadIdx.x; f <= mine; f += blockDim.x) {
+                float PL[5], PR[5], Fh[5];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    float v[2 * G];
+#pragma unroll
+                    for (int c = 0; c < 2 * G; ++c) v[c] = Ps[q * W + f + c];
+                    recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
+                }
+                const float nx[3] = {1.f, 0.f, 0.f};
+                hydro_face_flux<RIEMANN>(g.gamma, PL, PR, nx, Fh);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) Fx[q * (m + 1) + f] = Fh[q];
+            }
+            __syncthreads();
+            // 4. divergence and RK combine, in place; U0 is the step's start
+            for (int i = threadIdx.x; i < mine; i += blockDim.x) {
+                float Unew[5];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    const float L = -(Fx[q * (m + 1) + i + 1] - Fx[q * (m + 1) + i]) * g.idx;
+                    const df Up = {Uh[q * m + i], Ul[q * m + i]};
+                    df U0 = Up;
+                    if (rk == 0) {
+                        U0h[q * m + i] = Up.hi;
+                        U0l[q * m + i] = Up.lo;
+                    } else {
+                        U0 = {U0h[q * m + i], U0l[q * m + i]};
+                    }
+                    const df Un = rk_combine(U0, Up, dtf * L, b, omb);
+                    Uh[q * m + i] = Un.hi;
+                    Ul[q * m + i] = Un.lo;
+                    Unew[q] = Un.hi;
+                }
+                if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
+            }
+            if (last) {
+                // this CTA's part of the new state's Courant step: the minimum
+                // of the valid zone steps, as block_min_to orders them
+                float v = (zdt > 0.f && zdt < 3.0e38f) ? zdt : 3.0e38f;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, off));
+                if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = v;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    float w = 3.0e38f;
+                    for (int k = 0; k < (int) (blockDim.x + 31) / 32; ++k) w = fminf(w, wmin[k]);
+                    red[0] = w;
+                }
+            }
+            // neighbours have read this CTA's primitives before they change,
+            // and every CTA's Courant part is in place
+            cluster.sync();
+        }
+        // the slots are next written in the last stage of the next step,
+        // after at least one more cluster barrier, which no CTA reaches
+        // before it has read them here
+        float mn = 3.0e38f;
+        for (int k = 0; k < C; ++k) mn = fminf(mn, cluster.map_shared_rank(red, k)[0]);
+        // no valid zone leaves the slot at its reset value, as in the fused path
+        bits = (unsigned long long) __double_as_longlong(mn < 3.0e38f ? (double) mn : DBL_MAX);
+        t += dt;
+        steps += 1;
+    }
+    for (int i = threadIdx.x; i < mine; i += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            gh[q * g.sU + z0 + i] = Uh[q * m + i];
+            gl[q * g.sU + z0 + i] = Ul[q * m + i];
+        }
+    }
+    if (r == 0 && threadIdx.x == 0) {
+        st->t = t;
+        st->steps = steps;
+        st->dt = dt;
+        st->dt_bits = used;
+        st->done = done;
+        *cfl_bits = bits;
+    }
+}
+
+} // namespace mara

@@ -680,6 +680,9 @@ int mara_gpu_courant(MaraGpuHandle* h, double* dt)
     return rc;
 }
 
+// steps per launch of the cluster form (a few ms of work at most)
+constexpr int CLUSTER_STEPS = 1024;
+
 // one driver-loop step: Courant step, dt, the RK stages, the clock
 static void enqueue_run_step(MaraGpuHandle* h, double cfl, double t_final)
 {
@@ -729,6 +732,17 @@ static int launches_per_run_step(MaraGpuHandle* h)
 
 static int enqueue_run(MaraGpuHandle* h, int max_steps, double cfl, double t_final)
 {
+    if (h->mixed && !h->timing && mixed_cluster_capable(h->mixed)) {
+        // a small 1-D grid: chunks of steps, each one launch on a cluster
+        for (int left = max_steps; left > 0; left -= CLUSTER_STEPS) {
+            const int k = left < CLUSTER_STEPS ? left : CLUSTER_STEPS;
+            const int rc = mixed_enqueue_cluster_steps(h->mixed, k, cfl, t_final, h->st, h->stream);
+            if (rc) return rc;
+            h->steps += k;
+            h->launches++;
+        }
+        return cuda_status(cudaGetLastError());
+    }
     const bool use_graph = !h->timing;
     if (use_graph && (h->graph_cfl != cfl || h->graph_tfinal != t_final)) {
         for (int g = 0; g < 2; ++g) if (h->graph[g]) { cudaGraphExecDestroy(h->graph[g]); h->graph[g] = nullptr; }

@@ -10,11 +10,13 @@
 //    doing FP32 flux CT, divergence, the FP32-pair RK combine and the
 //    primitive recovery (FP32 for hydro and MHD, FP64 Newton for RMHD), and
 //    writing FP32 primitives with their guard images for the next sweep.
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 #include <vector>
 
 #include "diagnostics.cuh"
+#include "hydro_cluster.cuh"
 #include "hydro_tile.cuh"
 #include "mixed.h"
 #include "physics_fp32.cuh"
@@ -462,6 +464,7 @@ struct MixedState {
     int* drot = nullptr;     // state buffer index (device)
     int rot = 0;             // host mirror for the general form's parity
     unsigned long long* dcfl = nullptr;
+    HGrid hgrid;             // host copy of the fused form's grid record
     int tx = 32, ty = 16;
     int ctas = 0;
     int timing = 0;
@@ -533,6 +536,7 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
         h.idx = F.idx[0];
         h.idy = F.idx[1];
         h.lmin = F.lmin;
+        m->hgrid = h;
         m->tx = G.n[1] > 1 ? 32 : 256;
         m->ty = G.n[1] > 1 ? 16 : 1;
         std::vector<TileRef> tiles;
@@ -842,6 +846,52 @@ int mixed_launches_per_step(const MixedState* m)
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s) { k_cfl_publish<<<1, 1, 0, s>>>(m->dcfl, st); }
 int mixed_parity(const MixedState* m) { return m->rot & 1; }
 bool mixed_fused(const MixedState* m) { return m->fused; }
+
+// ---- small 1-D grids: many steps per launch on one thread-block cluster -------
+bool mixed_cluster_capable(const MixedState* m)
+{
+    return m->fused && m->G.n[1] == 1 && m->G.n[2] == 1 &&
+           m->G.n[0] <= CLUSTER1D_MAX_CTAS * CLUSTER1D_MAX_ZONES_PER_CTA;
+}
+
+template <int RECON, int RIEMANN>
+static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
+{
+    constexpr int G = HaloOf<RECON>::G;
+    const int n = m->G.n[0];
+    const int C = std::min(CLUSTER1D_MAX_CTAS, std::max(1, n / 128));  // every CTA owns >= 128 zones
+    const int mz = (n + C - 1) / C;
+    const size_t smem = cluster1d_smem_bytes(mz, G);
+    const int threads = std::min(1024, ((mz + 1 + 31) / 32) * 32);     // one thread per face
+    auto k = hydro_cluster1d_kernel<RECON, RIEMANN>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem) != cudaSuccess)
+        return MARA_ERR_CUDA;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned) C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned) C);
+    lc.blockDim = dim3((unsigned) threads);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&lc, k, m->hgrid, host_rot(m), m->cfg.rk_order, nsteps, cfl, t_final,
+                                             st, m->dcfl);
+    return e == cudaSuccess ? MARA_OK : MARA_ERR_CUDA;
+}
+
+int mixed_enqueue_cluster_steps(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
+{
+    const bool hllc = m->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (m->cfg.recon == MARA_RECON_PCM)
+        return hllc ? cluster_launch<RECON_PCM, RIEMANN_HLLC>(m, nsteps, cfl, t_final, st, s)
+                    : cluster_launch<RECON_PCM, RIEMANN_HLLE>(m, nsteps, cfl, t_final, st, s);
+    return hllc ? cluster_launch<RECON_PLM, RIEMANN_HLLC>(m, nsteps, cfl, t_final, st, s)
+                : cluster_launch<RECON_PLM, RIEMANN_HLLE>(m, nsteps, cfl, t_final, st, s);
+}
 void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
 void mixed_advance_parity(MixedState* m) { if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1; }
 void mixed_set_timing(MixedState* m, int on) { m->timing = on; }

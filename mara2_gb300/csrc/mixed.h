@@ -27,6 +27,11 @@ bool mixed_enqueue_run_step(MixedState* m, double cfl, double t_final, DevStatus
 bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t s);
 int mixed_launches_per_step(const MixedState* m);
 bool mixed_fused(const MixedState* m);
+// 1-D hydro grids of up to 8192 zones on the fused form: up to nsteps
+// driver-loop steps in one launch on a thread-block cluster holding the grid
+// in shared memory (hydro_cluster.cuh)
+bool mixed_cluster_capable(const MixedState* m);
+int mixed_enqueue_cluster_steps(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s);
 int mixed_parity(const MixedState* m);
 void mixed_set_parity(MixedState* m, int p);
 void mixed_advance_parity(MixedState* m);

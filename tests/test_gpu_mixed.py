@@ -98,3 +98,63 @@ def test_kernel_timing_counts_stage_launches(gpu_lib):
         g.set_kernel_timing(False)
     assert n[0] == 4 * s.rk_order, n
     assert ms[0] > 0.0
+
+
+def _riemann_1d(n, bc, recon, riemann, rk):
+    r = W.riemann_stream(1, seed=W.RIEMANN_SEED + 3)[0]
+    r.n, r.dims = n, 1
+    s, P = W.riemann_initial(r)
+    s = s.with_(bc=bc, recon=recon, riemann=riemann, rk_order=rk, guard=2)
+    return s, W.apply_bc_numpy(s, P)
+
+
+CLUSTER_CASES = [(256, "outflow", "plm", "hlle", 2), (1000, "periodic", "plm", "hllc", 3),
+                 (777, "reflecting", "pcm", "hllc", 1), (8192, "outflow", "plm", "hllc", 2),
+                 (131, "periodic", "pcm", "hlle", 2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,bc,recon,riemann,rk", CLUSTER_CASES)
+def test_cluster_run_matches_tile_steps(gpu_lib, n, bc, recon, riemann, rk):
+    """A 1-D grid's driver loop on one thread-block cluster (the grid held in
+    shared memory across many steps) against the same steps taken one launch
+    per stage by the tile kernels: the same clock and step count, and states
+    equal to FP32 rounding."""
+    s, P = _riemann_1d(n, bc, recon, riemann, rk)
+    steps = 40
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        taken = g.run(steps, s.cfl)
+        a = g.download()
+        t_cluster = g.t
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        t = 0.0
+        for _ in range(steps):
+            dt = g.courant() * s.cfl
+            g.advance(dt)
+            t += dt
+        b = g.download()
+    assert taken == steps
+    assert abs(t_cluster - t) <= 1e-6 * t
+    err = rel_l1(a[s.interior()], b[s.interior()])
+    assert err[0] < 1e-6 and err[4] < 1e-6, err
+
+
+@pytest.mark.gpu
+def test_cluster_run_stops_at_t_final_and_continues(gpu_lib, port):
+    """Runs that end at t_final inside a launch, and a second run that picks
+    up the clock and the Courant step the first one left."""
+    s, P = W.sod(1024)
+    c = oracle_config(s)
+    ref = P.copy()
+    _, t_ref, dts = port.run(c, ref, 100_000, s.cfl, s.t_final)
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        n1 = g.run(100, s.cfl, s.t_final)
+        n2 = g.run(100_000, s.cfl, s.t_final)
+        out = g.download()
+        assert abs(g.t - s.t_final) < 1e-12
+    assert n1 == 100 and abs((n1 + n2) - len(dts)) <= 2
+    err = rel_l1(out[s.interior()], ref[s.interior()])
+    assert err[0] < 1e-4, err
