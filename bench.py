@@ -310,7 +310,8 @@ def workload_suite(device: int, serving_requests: int = 512):
         "plain_fp64_zone_updates_per_s": s.zones * res["fp64"][1] / res["fp64"][2],
         "steps_mixed": res["mixed"][1], "steps_fp64": res["fp64"][1],
         "l1_density_vs_fp64_at_t_final": _l1_rho(res["fp64"][0], res["mixed"][0], s),
-        "note": "launch-bound: 1024 zones per step"}
+        "note": "mixed: the whole run on one thread-block cluster (grid in shared memory, 1024 steps per launch); "
+                "plain FP64: three kernels per step"}
 
     # 3. 3-D MHD turbulence with CT, 256^3, RK3
     s, P0 = W.mhd_turbulence(256)
