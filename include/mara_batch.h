@@ -41,6 +41,8 @@ typedef struct MaraBatchConfig {
     int rk_order;              /* 1, 2, 3                                   */
     int tile_1d;               /* zones per 1-D tile: 128, 256, 512, 0=auto */
     int tile_2d;               /* 2-D tile: 0=auto, 1=32x8, 2=32x16, 3=64x8 */
+    int lockstep_1d;           /* 1: small 1-D grids step with the tile lists
+                                  (0: on thread-block clusters, see below)  */
 } MaraBatchConfig;
 
 typedef struct MaraBatchStats {
@@ -66,7 +68,14 @@ int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* grid, const double* P_ao
                      int* slot);
 
 /* Enqueue `steps` batch steps: every active grid advances one time step with
- * its own dt; grids that reach t_final stop.  Asynchronous. */
+ * its own dt; grids that reach t_final stop.  Asynchronous.
+ *
+ * Unless lockstep_1d is set, a 1-D grid of at most 8192 zones is not in the
+ * tile lists: it runs its own driver loop on a thread-block cluster that
+ * holds it in shared memory, on a side stream concurrent with the batch
+ * steps.  Each call advances such a grid by a number of steps adapted so
+ * that the clusters take about as long as the call's batch steps (by 1024
+ * when no grid is in the tile lists).  Its results are the same bits. */
 int mara_batch_step(MaraBatch* b, int steps);
 
 /* Wait for the enqueued steps and list the slots that have reached t_final

@@ -32,7 +32,7 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotu
 class MaraBatchConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_int64), ("max_grids", C.c_int),
                 ("max_zones_per_grid", C.c_int), ("recon", C.c_int), ("riemann", C.c_int),
-                ("rk_order", C.c_int), ("tile_1d", C.c_int), ("tile_2d", C.c_int)]
+                ("rk_order", C.c_int), ("tile_1d", C.c_int), ("tile_2d", C.c_int), ("lockstep_1d", C.c_int)]
 
 
 class MaraBatchStats(C.Structure):
@@ -66,12 +66,13 @@ def load():
 class Batch:
     def __init__(self, budget_bytes: int, max_grids: int = 4096, max_zones_per_grid: int = 600 * 600,
                  recon: str = "plm", riemann: str = "hllc", rk_order: int = 2, tile_1d: int = 0,
-                 tile_2d: int = 0, device: int = 0):
+                 tile_2d: int = 0, device: int = 0, lockstep_1d: bool = False):
         self.lib = load()
         c = MaraBatchConfig()
         c.device, c.hbm_budget_bytes, c.max_grids = device, int(budget_bytes), max_grids
         c.max_zones_per_grid, c.recon, c.riemann = max_zones_per_grid, N.RECON[recon], N.RIEMANN[riemann]
         c.rk_order, c.tile_1d, c.tile_2d = rk_order, tile_1d, tile_2d
+        c.lockstep_1d = int(lockstep_1d)
         self.cfg = c
         h = C.c_void_p()
         N.check(self.lib.mara_batch_create(C.byref(c), C.byref(h)), "mara_batch_create")
@@ -171,7 +172,8 @@ class ServeResult:
 
 
 def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bool = False,
-          max_grids: int = 4096, tile_1d: int = 0, tile_2d: int = 0, device: int = 0, make=None) -> ServeResult:
+          max_grids: int = 4096, tile_1d: int = 0, tile_2d: int = 0, device: int = 0, make=None,
+          lockstep_1d: bool = False) -> ServeResult:
     """Continuous batching of `requests` (objects with .arrival seconds and a
     way to build (Scheme, P) through `make(req)`), arrivals replayed against
     the wall clock."""
@@ -183,7 +185,7 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bo
     res = ServeResult()
     max_cells = max(int(np.prod(make(r)[0].full_shape[:3])) for r in [max(requests, key=lambda r: r.zones())])
     with Batch(budget_bytes, max_grids=max_grids, max_zones_per_grid=max_cells, tile_1d=tile_1d,
-               tile_2d=tile_2d, device=device) as b:
+               tile_2d=tile_2d, device=device, lockstep_1d=lockstep_1d) as b:
         t0 = time.perf_counter()
         while pending or queue or inflight:
             now = time.perf_counter() - t0

@@ -19,11 +19,13 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "../../include/mara_batch.h"
+#include "hydro_cluster.cuh"
 #include "hydro_tile.cuh"
 
 namespace mara {
@@ -37,10 +39,37 @@ struct SlotHost {
     int64_t bytes = 0;
     float* bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int64_t zones = 0;
+    bool cluster = false;   // advanced on its own thread-block cluster (a small 1-D grid with an end time)
+    int bucket = 0;         // its zones-per-CTA class
 };
 
+// Small 1-D grids with an end time run their driver loop on thread-block
+// clusters (hydro_cluster.cuh) launched on side streams, K steps per batch
+// step call, instead of stepping in lockstep with the tile lists: a 1-D
+// request can need a hundred times the steps of the 2-D ones, and in
+// lockstep each of its steps would cost a whole batch step.  All clusters
+// of one launch have the same size, and every CTA the shared memory of the
+// launch's largest grid, so the grids are grouped in classes of (CTAs per
+// cluster, most zones per CTA): a grid of n zones takes the largest
+// power-of-two C <= n / 128 (1 to 8), and ceil(n / C) zones per CTA.  The
+// arithmetic of a zone does not depend on C.
+constexpr int CLUSTER_BUCKETS = 6;
+static const int CLUSTER_BUCKET_C[CLUSTER_BUCKETS] = {1, 2, 4, 8, 8, 8};
+static const int CLUSTER_BUCKET_M[CLUSTER_BUCKETS] = {256, 256, 256, 256, 512, 1024};
+constexpr int CLUSTER_MAX_ZONES = 8 * 1024;
+constexpr int CLUSTER_RUNNING = 3;  // done[] of a slot its cluster advances
+
+static int cluster_bucket(int n)
+{
+    if (n < 256) return 0;
+    if (n < 512) return 1;
+    if (n < 1024) return 2;
+    const int m = (n + 7) / 8;
+    return m <= 256 ? 3 : m <= 512 ? 4 : 5;
+}
+
 __global__ void k_slot_init(HGrid* grids, int* rot, double* t, double* dt, double* tfin, double* cflp, int* done,
-                            long long* steps, int* pend, int slot, HGrid g, double t_final, double cfl)
+                            long long* steps, int* pend, int slot, HGrid g, double t_final, double cfl, int done0)
 {
     grids[slot] = g;
     rot[slot] = 0;
@@ -48,7 +77,7 @@ __global__ void k_slot_init(HGrid* grids, int* rot, double* t, double* dt, doubl
     dt[slot] = 0.0;
     tfin[slot] = t_final;
     cflp[slot] = cfl;
-    done[slot] = 0;
+    done[slot] = done0;
     steps[slot] = 0;
     pend[slot] = 0;
 }
@@ -169,6 +198,21 @@ struct MaraBatch {
     int tile1 = 256, tile2 = 2;
     int ctas[2] = {0, 0};
     int count[2] = {0, 0};  // tiles in each list (host copy)
+    // cluster slots: per class, the device list, its pinned staging
+    // (double-buffered with the tile lists) and count; side streams; round
+    // events (main stream start and graph end, each class's end); steps per
+    // round of the cluster slots, adapted to the main stream's round time
+    bool clusters = true;
+    int* cl_slots[CLUSTER_BUCKETS] = {};
+    int* cl_host[CLUSTER_BUCKETS][2] = {};
+    int cl_count[CLUSTER_BUCKETS] = {};
+    cudaStream_t side[CLUSTER_BUCKETS] = {};
+    cudaEvent_t ev_start = nullptr, ev_main_end = nullptr;
+    cudaEvent_t ev_side_end[CLUSTER_BUCKETS] = {};
+    bool round_open = false;   // a round's events await reading
+    int round_mask = 0;        // the tile lists that round launched
+    bool round_side[CLUSTER_BUCKETS] = {};
+    int cl_steps[CLUSTER_BUCKETS] = {};
     // one captured step per combination of non-empty tile lists (bit 0: 1-D,
     // bit 1: 2-D), so that a step launches only the lists that hold tiles
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -251,15 +295,71 @@ static int launches_per_step(const MaraBatch* b)
     return 1 + b->cfg.rk_order * ((mask & 1) + ((mask >> 1) & 1));
 }
 
+// one launch advancing every grid of cluster class k by nsteps steps, on
+// the class's side stream
+template <int RECON, int RIEMANN>
+static cudaError_t launch_class(MaraBatch* b, int k, int nsteps)
+{
+    Cluster1DJob job = {};
+    job.grids = b->grids;
+    job.slots = b->cl_slots[k];
+    job.t = b->t;
+    job.steps = b->steps;
+    job.dt = b->dt;
+    job.done = b->done;
+    job.cfl = b->cflbits;
+    job.tfin = b->tfin;
+    job.cflp = b->cflp;
+    job.done_value = 2;
+    job.order = b->cfg.rk_order;
+    job.nsteps = nsteps;
+    job.buffer = 0;   // no rotation: the clusters update in place
+    return launch_cluster1d<RECON, RIEMANN>(job, b->cl_count[k], CLUSTER_BUCKET_C[k], CLUSTER_BUCKET_M[k],
+                                            b->side[k]);
+}
+
+static cudaError_t launch_cluster_class(MaraBatch* b, int k, int nsteps)
+{
+    const bool hllc = b->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (b->cfg.recon == MARA_RECON_PCM)
+        return hllc ? launch_class<RECON_PCM, RIEMANN_HLLC>(b, k, nsteps)
+                    : launch_class<RECON_PCM, RIEMANN_HLLE>(b, k, nsteps);
+    return hllc ? launch_class<RECON_PLM, RIEMANN_HLLC>(b, k, nsteps)
+                : launch_class<RECON_PLM, RIEMANN_HLLE>(b, k, nsteps);
+}
+
+// steps per round of the cluster classes: about as long as the round's batch
+// steps (damped: the clusters and the tile kernels share the SMs)
+static void adapt_cluster_steps(MaraBatch* b)
+{
+    if (!b->round_open) return;
+    b->round_open = false;
+    float main_ms = 0.f;
+    if (!b->round_mask || cudaEventElapsedTime(&main_ms, b->ev_start, b->ev_main_end) != cudaSuccess) return;
+    for (int k = 0; k < CLUSTER_BUCKETS; ++k) {
+        float side_ms = 0.f;
+        if (!b->round_side[k] || cudaEventElapsedTime(&side_ms, b->ev_start, b->ev_side_end[k]) != cudaSuccess ||
+            !(side_ms > 0.f))
+            continue;
+        const double f = std::sqrt((double) main_ms / side_ms);
+        b->cl_steps[k] = (int) std::min(4096.0, std::max(16.0, b->cl_steps[k] * f));
+    }
+}
+
 static int upload_tiles(MaraBatch* b)
 {
     // rebuild both lists from the resident grids into the free pinned buffer
     const int which = b->tiles_buf ^ 1;
     BK(cudaEventSynchronize(b->tiles_ev[which]));
     int count[2] = {0, 0};
+    int ccount[CLUSTER_BUCKETS] = {};
     for (int sl = 0; sl < b->nslots; ++sl) {
         const SlotHost& h = b->slots[sl];
         if (!h.used || h.finished_reported) continue;
+        if (h.cluster) {
+            b->cl_host[h.bucket][which][ccount[h.bucket]++] = sl;
+            continue;
+        }
         const int d = h.dims - 1;
         int tx, ty, nt;
         tile_dims(b, h.dims, &tx, &ty, &nt);
@@ -274,6 +374,11 @@ static int upload_tiles(MaraBatch* b)
                                          cudaMemcpyHostToDevice, b->stream));
         k_set_int<<<1, 1, 0, b->stream>>>(b->ntiles + d, count[d]);
         b->count[d] = count[d];
+    }
+    for (int k = 0; k < CLUSTER_BUCKETS; ++k) {
+        if (ccount[k]) BK(cudaMemcpyAsync(b->cl_slots[k], b->cl_host[k][which], sizeof(int) * ccount[k],
+                                          cudaMemcpyHostToDevice, b->stream));
+        b->cl_count[k] = ccount[k];
     }
     BK(cudaEventRecord(b->tiles_ev[which], b->stream));
     b->tiles_buf = which;
@@ -299,6 +404,8 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
     b->nslots = c->max_grids;
     b->tile1 = (c->tile_1d == 128 || c->tile_1d == 256 || c->tile_1d == 512) ? c->tile_1d : 256;
     b->tile2 = (c->tile_2d >= 1 && c->tile_2d <= 3) ? c->tile_2d : 2;
+    b->clusters = !c->lockstep_1d;
+    for (int k = 0; k < CLUSTER_BUCKETS; ++k) b->cl_steps[k] = 256;
     b->slots.resize(b->nslots);
     b->done_host.assign(b->nslots, 1);
     int rc = MARA_OK;
@@ -334,6 +441,15 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
     A((void**) &b->staging, sizeof(double) * b->staging_elems);
     for (int w = 0; w < 2 && !rc; ++w)
         if (cudaEventCreateWithFlags(&b->tiles_ev[w], cudaEventDisableTiming) != cudaSuccess) rc = MARA_ERR_CUDA;
+    for (int k = 0; k < CLUSTER_BUCKETS && !rc; ++k) {
+        A((void**) &b->cl_slots[k], sizeof(int) * n);
+        for (int w = 0; w < 2 && !rc; ++w)
+            if (cudaMallocHost((void**) &b->cl_host[k][w], sizeof(int) * n) != cudaSuccess) rc = MARA_ERR_CUDA;
+        if (!rc && cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking) != cudaSuccess) rc = MARA_ERR_CUDA;
+        if (!rc && cudaEventCreate(&b->ev_side_end[k]) != cudaSuccess) rc = MARA_ERR_CUDA;
+    }
+    if (!rc && (cudaEventCreate(&b->ev_start) != cudaSuccess || cudaEventCreate(&b->ev_main_end) != cudaSuccess))
+        rc = MARA_ERR_CUDA;
     if (!rc) {
         cudaMemsetAsync(b->done, 0, sizeof(int) * n, b->stream);
         std::vector<int> ones(n, 1);
@@ -359,6 +475,14 @@ int mara_batch_destroy(MaraBatch* b)
     if (!b) return MARA_OK;
     cudaSetDevice(b->cfg.device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    for (int k = 0; k < CLUSTER_BUCKETS; ++k) {
+        if (b->side[k]) { cudaStreamSynchronize(b->side[k]); cudaStreamDestroy(b->side[k]); }
+        if (b->ev_side_end[k]) cudaEventDestroy(b->ev_side_end[k]);
+        cudaFree(b->cl_slots[k]);
+        for (int w = 0; w < 2; ++w) if (b->cl_host[k][w]) cudaFreeHost(b->cl_host[k][w]);
+    }
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
+    if (b->ev_main_end) cudaEventDestroy(b->ev_main_end);
     for (auto& g : b->graph) if (g) cudaGraphExecDestroy(g);
     cudaFree(b->pend);
     for (auto& h : b->slots)
@@ -412,6 +536,8 @@ int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* c, const double* P_aos, 
     h.gamma = c->gamma;
     h.bytes = bytes;
     h.zones = zones;
+    h.cluster = b->clusters && dims == 1 && c->ni <= CLUSTER_MAX_ZONES && t_final >= 0.0;
+    h.bucket = h.cluster ? cluster_bucket(c->ni) : 0;
     b->bytes_in_use += bytes;
 
     HGrid g;
@@ -431,7 +557,7 @@ int mara_batch_admit(MaraBatch* b, const MaraGpuConfig* c, const double* P_aos, 
 
     BK(cudaMemcpyAsync(b->staging, P_aos, sizeof(double) * (size_t) N0 * N1 * 5, cudaMemcpyHostToDevice, b->stream));
     k_slot_init<<<1, 1, 0, b->stream>>>(b->grids, b->rot, b->t, b->dt, b->tfin, b->cflp, b->done, b->steps, b->pend,
-                                        sl, g, t_final, cfl);
+                                        sl, g, t_final, cfl, h.cluster ? CLUSTER_RUNNING : 0);
     k_set_u64<<<1, 1, 0, b->stream>>>(b->cflbits + sl, ~0ull);
     dim3 grid((c->ni + 255) / 256, c->nj);
     k_batch_load<<<grid, 256, 0, b->stream>>>(b->staging, g, h.g0, h.g1, N0, N1, 1.0 / (c->gamma - 1.0),
@@ -462,7 +588,29 @@ int mara_batch_step(MaraBatch* b, int steps)
         cudaGraphDestroy(g);
         BK(e);
     }
+    // the cluster classes first, so that their CTAs are placed while the
+    // batch steps queue behind them on the main stream
+    bool side = false;
+    for (int k = 0; k < CLUSTER_BUCKETS; ++k) side = side || b->cl_count[k] > 0;
+    if (side && steps > 0) {
+        BK(cudaEventRecord(b->ev_start, b->stream));
+        for (int k = 0; k < CLUSTER_BUCKETS; ++k) {
+            b->round_side[k] = b->cl_count[k] > 0;
+            if (!b->round_side[k]) continue;
+            BK(cudaStreamWaitEvent(b->side[k], b->ev_start, 0));
+            BK(launch_cluster_class(b, k, mask ? b->cl_steps[k] : 1024));
+            BK(cudaEventRecord(b->ev_side_end[k], b->side[k]));
+            b->launches += 1;
+        }
+    }
     for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph[mask], b->stream));
+    if (side && steps > 0) {
+        BK(cudaEventRecord(b->ev_main_end, b->stream));
+        for (int k = 0; k < CLUSTER_BUCKETS; ++k)
+            if (b->round_side[k]) BK(cudaStreamWaitEvent(b->stream, b->ev_side_end[k], 0));
+        b->round_open = true;
+        b->round_mask = mask;
+    }
     b->step_count += steps;
     b->launches += (int64_t) steps * launches_per_step(b);
     return MARA_OK;
@@ -475,6 +623,7 @@ int mara_batch_poll(MaraBatch* b, int* slots, int cap, int* n)
     std::vector<int> d(b->nslots);
     BK(cudaMemcpyAsync(d.data(), b->done, sizeof(int) * b->nslots, cudaMemcpyDeviceToHost, b->stream));
     BK(cudaStreamSynchronize(b->stream));
+    adapt_cluster_steps(b);
     int m = 0;
     for (int k = 0; k < b->nslots; ++k) {
         SlotHost& h = b->slots[k];

@@ -35,21 +35,46 @@ __host__ __device__ constexpr size_t cluster1d_smem_bytes(int m, int G)
     return sizeof(float) * (4 * 5 * (size_t) m + 5 * (size_t) (m + 2 * G) + 5 * (size_t) (m + 1) + 4);
 }
 
-// Driver-loop steps (at most nsteps, stopping at t_final when t_final >= 0)
-// of the grid g, whose state is buffer s of its rotation; the state is
-// written back to buffer s.  st holds the clock (t, steps, dt, done) as the
-// graph-replayed steps keep it; *cfl_bits holds the Courant step of the state
-// (bits of a positive double) on entry and on exit.
+// What one launch advances: cluster c of the launch runs the driver loop of
+// slot slots[c] (slot 0 when slots is null) of the tables below, at most
+// nsteps steps, stopping at t_final (t_final < 0: no end time).  The tables
+// are the handle's status (one slot) or the batch's per-grid arrays.
+struct Cluster1DJob {
+    const HGrid* grids;          // grid records (device)
+    const int* slots;            // slot of each cluster, or null
+    double* t;                   // clock, per slot
+    long long* steps;
+    double* dt;
+    int* done;                   // done_value once t reached t_final
+    unsigned long long* used;    // the Courant step the last dt came from (may be null)
+    unsigned long long* cfl;     // Courant step of the state (bits of a positive double)
+    const double* tfin;          // per-slot end times, or null: t_final below
+    const double* cflp;          // per-slot CFL numbers, or null: cfl_number below
+    double t_final, cfl_number;
+    int done_value;
+    int order;                   // RK order
+    int nsteps;
+    int buffer;                  // the state's buffer in the grid's rotation
+};
+
+// Driver-loop steps of small 1-D grids; the state is read from and written
+// back to buffer job.buffer of each grid's rotation.  Clusters of one launch
+// may hold grids of different sizes: each CTA uses the zones of its own grid
+// (at most the m the launch's shared memory was sized for).
 template <int RECON, int RIEMANN>
-__global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(HGrid g, int s, int order, int nsteps, double cfl,
-                                                               double t_final, DevStatus* __restrict__ st,
-                                                               unsigned long long* __restrict__ cfl_bits)
+__global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
 {
     namespace cg = cooperative_groups;
     constexpr int G = HaloOf<RECON>::G;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int) cluster.num_blocks();
     const int r = (int) cluster.block_rank();
+    const int slot = job.slots ? job.slots[blockIdx.x / C] : 0;
+    const HGrid& g = job.grids[slot];
+    const int s = job.buffer;
+    const int order = job.order;
+    const double cfl = job.cflp ? job.cflp[slot] : job.cfl_number;
+    const double t_final = job.tfin ? job.tfin[slot] : job.t_final;
     const int n = g.n0;
     const int m = (n + C - 1) / C;                 // zones per CTA
     const int z0 = r * m;
@@ -76,15 +101,15 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(HGrid g, int s, i
         }
     }
     // every CTA follows the same clock: the same doubles from the same inputs
-    double t = st->t;
-    long long steps = st->steps;
-    int done = st->done;
-    double dt = st->dt;
-    unsigned long long bits = *cfl_bits;
-    unsigned long long used = st->dt_bits;       // the Courant step the last dt came from
+    double t = job.t[slot];
+    long long steps = job.steps[slot];
+    int done = job.done[slot] == job.done_value;
+    double dt = job.dt[slot];
+    unsigned long long bits = job.cfl[slot];
+    unsigned long long used = job.used ? job.used[slot] : 0ull;
     cluster.sync();
 
-    for (int step = 0; step < nsteps && !done; ++step) {
+    for (int step = 0; step < job.nsteps && !done; ++step) {
         // the step start of the fused path (k_fused_run_begin)
         used = bits;
         dt = cfl * __longlong_as_double((long long) bits);
@@ -192,6 +217,9 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(HGrid g, int s, i
         bits = (unsigned long long) __double_as_longlong(mn < 3.0e38f ? (double) mn : DBL_MAX);
         t += dt;
         steps += 1;
+        // the next step's start would stop here: stop now, so that a grid
+        // finishing on a launch's last step is reported by that launch
+        if (t_final >= 0.0 && !(t < t_final)) done = 1;
     }
     for (int i = threadIdx.x; i < mine; i += blockDim.x) {
 #pragma unroll
@@ -200,14 +228,50 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(HGrid g, int s, i
             gl[q * g.sU + z0 + i] = Ul[q * m + i];
         }
     }
+    // the clock is published after every CTA's part of the state
+    __threadfence();
+    cluster.sync();
     if (r == 0 && threadIdx.x == 0) {
-        st->t = t;
-        st->steps = steps;
-        st->dt = dt;
-        st->dt_bits = used;
-        st->done = done;
-        *cfl_bits = bits;
+        job.t[slot] = t;
+        job.steps[slot] = steps;
+        job.dt[slot] = dt;
+        if (job.used) job.used[slot] = used;
+        job.cfl[slot] = bits;
+        __threadfence();
+        if (done) job.done[slot] = job.done_value;
     }
+}
+
+// grid of cluster_count clusters of C CTAs, each CTA sized for up to m zones
+template <int RECON, int RIEMANN>
+inline cudaError_t launch_cluster1d(const Cluster1DJob& job, int cluster_count, int C, int m, cudaStream_t stream)
+{
+    constexpr int G = HaloOf<RECON>::G;
+    const size_t smem = cluster1d_smem_bytes(m, G);
+    const int threads = m + 1 < 1024 ? ((m + 1 + 31) / 32) * 32 : 1024;  // one thread per face
+    auto k = hydro_cluster1d_kernel<RECON, RIEMANN>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned) C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned) (cluster_count * C));
+    lc.blockDim = dim3((unsigned) threads);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = stream;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, k, job);
+}
+
+// CTAs of a grid of n zones: every CTA owns at least 128 zones
+inline int cluster1d_ctas(int n)
+{
+    const int c = n / 128;
+    return c < 1 ? 1 : c > CLUSTER1D_MAX_CTAS ? CLUSTER1D_MAX_CTAS : c;
 }
 
 } // namespace mara

@@ -464,7 +464,6 @@ struct MixedState {
     int* drot = nullptr;     // state buffer index (device)
     int rot = 0;             // host mirror for the general form's parity
     unsigned long long* dcfl = nullptr;
-    HGrid hgrid;             // host copy of the fused form's grid record
     int tx = 32, ty = 16;
     int ctas = 0;
     int timing = 0;
@@ -536,7 +535,6 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
         h.idx = F.idx[0];
         h.idy = F.idx[1];
         h.lmin = F.lmin;
-        m->hgrid = h;
         m->tx = G.n[1] > 1 ? 32 : 256;
         m->ty = G.n[1] > 1 ? 16 : 1;
         std::vector<TileRef> tiles;
@@ -857,29 +855,23 @@ bool mixed_cluster_capable(const MixedState* m)
 template <int RECON, int RIEMANN>
 static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
 {
-    constexpr int G = HaloOf<RECON>::G;
     const int n = m->G.n[0];
-    const int C = std::min(CLUSTER1D_MAX_CTAS, std::max(1, n / 128));  // every CTA owns >= 128 zones
-    const int mz = (n + C - 1) / C;
-    const size_t smem = cluster1d_smem_bytes(mz, G);
-    const int threads = std::min(1024, ((mz + 1 + 31) / 32) * 32);     // one thread per face
-    auto k = hydro_cluster1d_kernel<RECON, RIEMANN>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem) != cudaSuccess)
-        return MARA_ERR_CUDA;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = (unsigned) C;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((unsigned) C);
-    lc.blockDim = dim3((unsigned) threads);
-    lc.dynamicSmemBytes = smem;
-    lc.stream = s;
-    lc.attrs = at;
-    lc.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&lc, k, m->hgrid, host_rot(m), m->cfg.rk_order, nsteps, cfl, t_final,
-                                             st, m->dcfl);
+    const int C = cluster1d_ctas(n);
+    Cluster1DJob job = {};
+    job.grids = m->dgrid;
+    job.t = &st->t;
+    job.steps = &st->steps;
+    job.dt = &st->dt;
+    job.done = &st->done;
+    job.used = &st->dt_bits;
+    job.cfl = m->dcfl;
+    job.t_final = t_final;
+    job.cfl_number = cfl;
+    job.done_value = 1;
+    job.order = m->cfg.rk_order;
+    job.nsteps = nsteps;
+    job.buffer = host_rot(m);
+    const cudaError_t e = launch_cluster1d<RECON, RIEMANN>(job, 1, C, (n + C - 1) / C, s);
     return e == cudaSuccess ? MARA_OK : MARA_ERR_CUDA;
 }
 

@@ -4,9 +4,12 @@ Each grid's arithmetic must not depend on the other grids in the batch or on
 where its tiles land: a request solved alone and the same request solved in a
 mix give bit-identical results and step counts; a grid solved in the batch
 matches the single-grid mixed path bit for bit."""
+import dataclasses
+
 import numpy as np
 import pytest
 
+from helpers import rel_l1
 from mara2_gb300 import workloads as W
 
 
@@ -41,6 +44,70 @@ def test_alone_equals_mix(gpu_lib):
         Pm, tm, nm = out[k]
         assert na == nm and ta == tm, (k, na, nm)
         assert np.array_equal(Pa[s.interior()].view(np.uint64), Pm[s.interior()].view(np.uint64)), k
+
+
+def _run_batch(built, **kw):
+    from mara2_gb300.batch import Batch
+    cells = max(int(np.prod(s.full_shape[:3])) for s, _ in built)
+    out = {}
+    with Batch(budget_bytes=1 << 29, max_grids=64, max_zones_per_grid=cells, **kw) as b:
+        slots = {b.admit(s, P, s.t_final): k for k, (s, P) in enumerate(built)}
+        while len(out) < len(built):
+            b.step(5)
+            for sl in b.poll():
+                k = slots[sl]
+                out[k] = b.retire(sl, built[k][0].full_shape)
+    return out
+
+
+@pytest.mark.gpu
+def test_cluster_slots_match_lockstep(gpu_lib):
+    """1-D grids of every cluster class (1 to 8 CTAs, up to 1024 zones per
+    CTA) run on their own clusters beside 2-D grids in the tile lists, against
+    all grids stepping in lockstep: the 2-D grids give the same bits, the 1-D
+    grids the same clock and step count and states equal to FP32 rounding
+    (the cluster kernel is a separately compiled FP32 kernel, whose multiply-
+    adds the compiler may fuse differently)."""
+    reqs = W.riemann_stream(40, rate=1e6, seed=5, n1=(64, 512), n2=(32, 64))
+    one = [r for r in reqs if r.dims == 1][:6]
+    two = [r for r in reqs if r.dims == 2][:4]
+    sizes = [100, 300, 700, 1500, 3000, 8192]
+    built = []
+    for r, n in zip(one, sizes):
+        s, P = W.riemann_initial(dataclasses.replace(r, n=n))
+        built.append((s.with_(t_final=0.004), P))
+    built += [_make(r) for r in two]
+    a = _run_batch(built)
+    b = _run_batch(built, lockstep_1d=True)
+    for k, (s, _) in enumerate(built):
+        Pa, ta, na = a[k]
+        Pb, tb, nb = b[k]
+        assert na == nb and abs(ta - tb) <= 1e-12 * tb, (k, na, nb, ta, tb)
+        if s.shape[1] > 1:
+            assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), k
+        else:
+            err = rel_l1(Pa[s.interior()], Pb[s.interior()])
+            assert err[0] < 1e-6 and err[4] < 1e-6, (k, err)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [300, 5000])
+def test_cluster_slot_matches_single_grid_run(gpu_lib, n):
+    """A 1-D grid in the batch and the same grid run by a single-grid handle
+    (both on a thread-block cluster): the same bits and step count."""
+    from mara2_gb300.batch import run_alone
+    from mara2_gb300.solver import Solver
+    r = next(r for r in W.riemann_stream(8, rate=1e6, seed=3) if r.dims == 1)
+    s, P = W.riemann_initial(dataclasses.replace(r, n=n))
+    s = s.with_(t_final=0.003)
+    Pb, tb, nb = run_alone(s, P, s.t_final)
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        ns = g.run(100_000, s.cfl, s.t_final)
+        Ps = g.download()
+        ts = g.t
+    assert ns == nb and ts == tb
+    assert np.array_equal(Pb[s.interior()].view(np.uint64), Ps[s.interior()].view(np.uint64))
 
 
 @pytest.mark.gpu
