@@ -159,6 +159,8 @@ class ServeResult:
     peak_active: int = 0
     peak_bytes: int = 0
     results: dict = field(default_factory=dict)
+    # per request, in completion order: (index, latency s, queue wait s, steps)
+    records: list = field(default_factory=list)
 
     def summary(self) -> dict:
         lat = np.array(self.latencies) if self.latencies else np.array([np.nan])
@@ -213,6 +215,7 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bo
                     res.queue_waits.append(t_admit - r.arrival)
                     res.zone_updates += s.zones * nsteps
                     res.completed += 1
+                    res.records.append((r.index, done_t - r.arrival, t_admit - r.arrival, nsteps))
                     if keep_results:
                         res.results[r.index] = (out, t, nsteps)
                 st = b.stats()
