@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                 float U[5], P[5];
 #pragma unroll
                 for (int q = 0; q < 5; ++q) U[q] = Uh[q * m + i];
-                hydro_cons_f(g.gamma, U, P);
+                fh_cons(g.gamma, U, P);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Ps[q * W + G + i] = P[q];
             }
@@ -163,8 +163,7 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                     for (int c = 0; c < 2 * G; ++c) v[c] = Ps[q * W + f + c];
                     recon_pair<RECON>(v, g.plm_theta, PL[q], PR[q]);
                 }
-                const float nx[3] = {1.f, 0.f, 0.f};
-                hydro_face_flux<RIEMANN>(g.gamma, PL, PR, nx, Fh);
+                hydro_face_flux<RIEMANN, 0>(g.gamma, PL, PR, Fh);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Fx[q * (m + 1) + f] = Fh[q];
             }
@@ -174,7 +173,7 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                 float Unew[5];
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
-                    const float L = -(Fx[q * (m + 1) + i + 1] - Fx[q * (m + 1) + i]) * g.idx;
+                    const float L = fh_div(Fx[q * (m + 1) + i], Fx[q * (m + 1) + i + 1], g.idx);
                     const df Up = {Uh[q * m + i], Ul[q * m + i]};
                     df U0 = Up;
                     if (rk == 0) {
@@ -183,7 +182,7 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                     } else {
                         U0 = {U0h[q * m + i], U0l[q * m + i]};
                     }
-                    const df Un = rk_combine(U0, Up, dtf * L, b, omb);
+                    const df Un = rk_combine(U0, Up, f_mul(dtf, L), b, omb);
                     Uh[q * m + i] = Un.hi;
                     Ul[q * m + i] = Un.lo;
                     Unew[q] = Un.hi;

@@ -84,6 +84,124 @@ __device__ __forceinline__ void hydro_u2p_d(const double* U, double gm1, double*
 
 template <int RECON> struct HaloOf { static constexpr int G = RECON == RECON_PCM ? 1 : 2; };
 
+// ---- the FP32 arithmetic of the fused kernels --------------------------------
+// Every operation is an explicitly rounded intrinsic or a PTX approximate
+// reciprocal / square root, so that no multiply and add are fused differently
+// in different kernels: the stage kernels, the cluster driver loop and the
+// pipelined host step give the same bits from the same state.
+__device__ __forceinline__ float f_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float f_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float f_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float f_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float f_rcp(float a)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+__device__ __forceinline__ float f_sqrt(float a)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+// NewtonianHydro::fromConserved (ConservationLaws.cpp:292-318) in FP32
+__device__ __forceinline__ void fh_cons(float gamma, const float* U, float* P)
+{
+    const float ir = f_rcp(U[0]);
+    const float mm = f_fma(U[3], U[3], f_fma(U[2], U[2], f_mul(U[1], U[1])));
+    P[0] = U[0];
+    P[1] = f_mul(U[1], ir);
+    P[2] = f_mul(U[2], ir);
+    P[3] = f_mul(U[3], ir);
+    P[4] = f_mul(f_fma(f_mul(-0.5f, mm), ir, U[4]), f_sub(gamma, 1.0f));
+}
+
+// NewtonianHydro::fromPrimitive (ConservationLaws.cpp:253-290) for the face
+// normal along axis AXIS
+template <int AXIS>
+__device__ __forceinline__ void fh_prim(float gamma, const float* P, StateF<5>& S)
+{
+    const float cs = f_sqrt(f_mul(f_mul(gamma, P[4]), f_rcp(P[0])));
+    const float vv = f_fma(P[3], P[3], f_fma(P[2], P[2], f_mul(P[1], P[1])));
+    const float vn = P[1 + AXIS];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) S.P[q] = P[q];
+    S.U[0] = P[0];
+    S.U[1] = f_mul(P[0], P[1]);
+    S.U[2] = f_mul(P[0], P[2]);
+    S.U[3] = f_mul(P[0], P[3]);
+    S.U[4] = f_fma(f_mul(0.5f, P[0]), vv, f_mul(P[4], f_rcp(f_sub(gamma, 1.0f))));
+    S.F[0] = f_mul(vn, S.U[0]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) S.F[1 + d] = d == AXIS ? f_fma(vn, S.U[1 + d], P[4]) : f_mul(vn, S.U[1 + d]);
+    S.F[4] = f_mul(vn, f_add(S.U[4], P[4]));
+    S.amax = fmaxf(f_add(vn, cs), 0.0f);
+    S.amin = fminf(f_sub(vn, cs), 0.0f);
+}
+
+// HlleRiemannSolver::solve (RiemannSolvers.cpp:38-57)
+__device__ __forceinline__ void fh_hlle(const StateF<5>& L, const StateF<5>& R, float* F)
+{
+    const float ap = fmaxf(L.amax, R.amax);
+    const float am = fminf(L.amin, R.amin);
+    const float id = f_rcp(f_sub(ap, am));
+    const float apam = f_mul(ap, am);
+#pragma unroll
+    for (int q = 0; q < 5; ++q)
+        F[q] = f_mul(f_fma(apam, f_sub(R.U[q], L.U[q]), f_fma(ap, L.F[q], f_mul(-am, R.F[q]))), id);
+}
+
+// the star-state flux of one side (RiemannSolvers.cpp:86-115): S the side's
+// wave speed, m = rho (S - vn)
+template <int AXIS>
+__device__ __forceinline__ void fh_hllc_star(const StateF<5>& K, float S, float m, float lc, float* F)
+{
+    const float* P = K.P;
+    const float vn = P[1 + AXIS];
+    const float f = f_mul(m, f_rcp(f_sub(S, lc)));
+    float Us[5];
+    Us[0] = f;
+    Us[4] = f_mul(f, f_fma(f_sub(lc, vn), f_add(lc, f_mul(P[4], f_rcp(m))), f_mul(K.U[4], f_rcp(P[0]))));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Us[1 + d] = d == AXIS ? f_mul(f, f_add(f_sub(lc, vn), P[1 + d])) : f_mul(f, P[1 + d]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) F[i] = f_fma(S, f_sub(Us[i], K.U[i]), K.F[i]);
+}
+
+// HllcNewtonianHydroRiemannSolver::solve (RiemannSolvers.cpp:63-118)
+template <int AXIS>
+__device__ __forceinline__ void fh_hllc(const StateF<5>& L, const StateF<5>& R, float* F)
+{
+    const float ap = fmaxf(L.amax, R.amax);
+    const float am = fminf(L.amin, R.amin);
+    const float vnl = L.P[1 + AXIS], vnr = R.P[1 + AXIS];
+    const float ml = f_mul(L.P[0], f_sub(am, vnl)), mr = f_mul(R.P[0], f_sub(ap, vnr));
+    const float lc = f_mul(f_sub(f_fma(-mr, vnr, R.P[4]), f_fma(-ml, vnl, L.P[4])), f_rcp(f_sub(ml, mr)));
+    if (0.0f <= am) {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) F[i] = L.F[i];
+    } else if (0.0f <= lc) {
+        fh_hllc_star<AXIS>(L, am, ml, lc, F);
+    } else if (0.0f <= ap) {
+        fh_hllc_star<AXIS>(R, ap, mr, lc, F);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) F[i] = R.F[i];
+    }
+}
+
+// generalized minmod (Reconstruction.cpp:55-61), see minmod_f
+__device__ __forceinline__ float fh_minmod(float theta, float ul, float u0, float ur)
+{
+    const float a = f_mul(theta, f_sub(u0, ul));
+    const float b = f_mul(0.5f, f_sub(ur, ul));
+    const float c = f_mul(theta, f_sub(ur, u0));
+    const float m = fminf(fabsf(a), fminf(fabsf(b), fabsf(c)));
+    return f_mul(a, c) > 0.0f ? copysignf(m, a) : 0.0f;
+}
+
 template <int RECON>
 __device__ __forceinline__ void recon_pair(const float* v, float theta, float& L, float& R)
 {
@@ -92,19 +210,20 @@ __device__ __forceinline__ void recon_pair(const float* v, float theta, float& L
         L = v[0];
         R = v[1];
     } else {
-        L = v[1] + 0.5f * minmod_f(theta, v[0], v[1], v[2]);
-        R = v[2] - 0.5f * minmod_f(theta, v[1], v[2], v[3]);
+        L = f_fma(0.5f, fh_minmod(theta, v[0], v[1], v[2]), v[1]);
+        R = f_fma(-0.5f, fh_minmod(theta, v[1], v[2], v[3]), v[2]);
     }
 }
 
-template <int RIEMANN>
-__device__ __forceinline__ void hydro_face_flux(float gamma, const float* PL, const float* PR, const float* n, float* F)
+// the flux through a face whose normal is along axis AXIS
+template <int RIEMANN, int AXIS>
+__device__ __forceinline__ void hydro_face_flux(float gamma, const float* PL, const float* PR, float* F)
 {
     StateF<5> L, R;
-    hydro_prim_f(gamma, PL, n, L);
-    hydro_prim_f(gamma, PR, n, R);
-    if constexpr (RIEMANN == RIEMANN_HLLC) hllc_f<5>(L, R, n, F);
-    else hlle_f<5>(L, R, F);
+    fh_prim<AXIS>(gamma, PL, L);
+    fh_prim<AXIS>(gamma, PR, R);
+    if constexpr (RIEMANN == RIEMANN_HLLC) fh_hllc<AXIS>(L, R, F);
+    else fh_hlle(L, R, F);
 }
 
 // Courant step of one zone: lmin / max over x, y, z of max |eigenvalue|
@@ -112,13 +231,21 @@ __device__ __forceinline__ void hydro_face_flux(float gamma, const float* PL, co
 __device__ __forceinline__ float hydro_zone_dt(float gamma, float lmin, const float* U)
 {
     float P[5];
-    hydro_cons_f(gamma, U, P);
-    const float cs = sqrtf(gamma * P[4] / P[0]);
+    fh_cons(gamma, U, P);
+    const float cs = f_sqrt(f_mul(f_mul(gamma, P[4]), f_rcp(P[0])));
     const float vmax = fmaxf(fabsf(P[1]), fmaxf(fabsf(P[2]), fabsf(P[3])));
-    return lmin / (vmax + cs);
+    return f_mul(lmin, f_rcp(f_add(vmax, cs)));
 }
 
 __device__ __forceinline__ float hydro_zone_dt(const HGrid& g, const float* U) { return hydro_zone_dt(g.gamma, g.lmin, U); }
+
+// the update of one field of one zone: L = -(F+ - F-) / dx (- (G+ - G-) / dy),
+// U = rk_combine(U0, U, dt L)
+__device__ __forceinline__ float fh_div(float fm, float fp, float idx) { return f_mul(f_sub(fm, fp), idx); }
+__device__ __forceinline__ float fh_div(float fm, float fp, float idx, float gm, float gp, float idy)
+{
+    return f_fma(f_sub(gm, gp), idy, fh_div(fm, fp, idx));
+}
 
 __device__ __forceinline__ void block_min_to(unsigned long long* dst, float v)
 {
@@ -132,9 +259,196 @@ __device__ __forceinline__ void block_min_to(unsigned long long* dst, float v)
     if ((threadIdx.x & 31) == 0 && b != ~0ull) atomicMin(dst, b);
 }
 
+// shared memory of one tile stage
+template <int DIM, int RECON, int TX, int TY>
+struct TileSmem {
+    static constexpr int G = HaloOf<RECON>::G;
+    float Ps[5][DIM == 2 ? TY + 2 * G : 1][TX + 2 * G];
+    float Fx[5][TY][TX + 1];
+    float Fy[5][DIM == 2 ? TY + 1 : 1][DIM == 2 ? TX : 1];
+};
+
+// a load of the state: through L1 in the stage kernels (nothing a stage
+// reads changes during its launch), from L2 where CTAs of one launch read
+// what other CTAs of it wrote
+template <bool L2ONLY>
+__device__ __forceinline__ float ld_state(const float* p)
+{
+    if constexpr (L2ONLY) return __ldcg(p);
+    else return *p;
+}
+
+// One RK stage of one tile of grid g whose state is in rotation buffer s:
+//   src: buffer holding the stage input; dst: buffer written; buffer s
+//   holds U0 (read per zone); b, omb = b, 1 - b; on the last stage the
+//   tile's Courant step goes to *at.cfl().  at.dt() and at.cfl() are read
+//   where they are used, so that neither holds registers across the tile.
+template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, class At>
+__device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, const HGrid& g, const TileRef& tr,
+                                           int s, int stage, float b, float omb, int last, const At& at)
+{
+    constexpr int G = HaloOf<RECON>::G;
+    constexpr int WX = TX + 2 * G;
+    constexpr int WY = DIM == 2 ? TY + 2 * G : 1;
+    constexpr int FXN = (TX + 1) * TY;
+    constexpr int FYN = DIM == 2 ? TX * (TY + 1) : 1;
+    // buffer rotation: stage input / output per RK stage
+    int src, dst;
+    if (stage == 0) { src = s; dst = last ? (s ^ 1) : (s + 1) % 3; }
+    else if (stage == 1) { src = (s + 1) % 3; dst = last ? s : (s + 2) % 3; }
+    else { src = (s + 2) % 3; dst = s; }
+    const float* __restrict__ Uin = g.Uh[src];
+    const long long sU = g.sU;
+    const int n0 = g.n0, n1 = g.n1;
+
+    // L2 prefetch of what the update phase reads per zone besides the
+    // stage input's high word (already staged below): its low word and,
+    // after the first stage, both words of U0
+    {
+        const int rows = DIM == 2 ? TY : 1;
+        const int per = (TX * 4 + 127) / 128;            // 128-byte lines per row segment
+        const int arrays = stage == 0 ? 1 : 3;
+        const int lines = arrays * 5 * rows * per;
+        for (int l = threadIdx.x; l < lines; l += NT) {
+            const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
+            const int y = tr.y0 + r, x = tr.x0 + seg * 32;
+            if (y < n1 && x < n0) {
+                const float* base = a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
+                const float* ptr = base + q * sU + (long long) y * n0 + x;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+            }
+        }
+    }
+
+    __syncthreads(); // the previous tile's shared data is consumed
+    // 1. primitives of the tile and its halo: all loads first, then the
+    //    conversions, so each thread keeps NC x 5 loads in flight.  A tile
+    //    whose halo lies inside the grid reads it as one rectangle; the
+    //    others take every halo zone from its boundary image.
+    {
+        constexpr int NC = (WX * WY + NT - 1) / NT;
+        float Ur[NC][5];
+        int fl[NC];
+        const bool inner = tr.x0 - G >= 0 && tr.x0 + TX + G <= n0 &&
+                           (DIM == 1 || (tr.y0 - G >= 0 && tr.y0 + TY + G <= n1));
+        if (inner) {
+            const float* base = Uin + (long long) (tr.y0 - (DIM == 2 ? G : 0)) * n0 + (tr.x0 - G);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const int c = threadIdx.x + k * NT;
+                fl[k] = 0;
+                if (c < WX * WY) {
+                    const int lx = c % WX, ly = c / WX;
+                    const float* p = base + (long long) ly * n0 + lx;
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(p + q * sU);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const int c = threadIdx.x + k * NT;
+                fl[k] = 0;
+                if (c < WX * WY) {
+                    const int lx = c % WX, ly = c / WX;
+                    int flipx = 0, flipy = 0;
+                    const int x = bc_image(tr.x0 + lx - G, n0, g.bc, flipx);
+                    const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, n1, g.bc, flipy) : 0;
+                    const long long o = (long long) y * n0 + x;
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(Uin + q * sU + o);
+                    fl[k] = flipx | (flipy << 1);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const int c = threadIdx.x + k * NT;
+            if (c < WX * WY) {
+                const int lx = c % WX, ly = c / WX;
+                if (fl[k] & 1) Ur[k][1] = -Ur[k][1];
+                if (fl[k] & 2) Ur[k][2] = -Ur[k][2];
+                float P[5];
+                fh_cons(g.gamma, Ur[k], P);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) sm.Ps[q][ly][lx] = P[q];
+            }
+        }
+    }
+    __syncthreads();
+
+    const float theta = g.plm_theta, gamma = g.gamma;
+    // 2. x faces and y faces in one balanced loop (face fx sits left of
+    //    tile zone fx, face fy below tile row fy)
+    for (int f = threadIdx.x; f < FXN + (DIM == 2 ? FYN : 0); f += NT) {
+        float PL[5], PR[5], Fh[5];
+        if (f < FXN) {
+            const int fx = f % (TX + 1), fy = f / (TX + 1);
+            const int ry = DIM == 2 ? fy + G : 0;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                float v[2 * G];
+#pragma unroll
+                for (int m = 0; m < 2 * G; ++m) v[m] = sm.Ps[q][ry][fx + m];
+                recon_pair<RECON>(v, theta, PL[q], PR[q]);
+            }
+            hydro_face_flux<RIEMANN, 0>(gamma, PL, PR, Fh);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) sm.Fx[q][fy][fx] = Fh[q];
+        } else if constexpr (DIM == 2) {
+            const int h = f - FXN;
+            const int fx = h % TX, fy = h / TX;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                float v[2 * G];
+#pragma unroll
+                for (int m = 0; m < 2 * G; ++m) v[m] = sm.Ps[q][fy + m][fx + G];
+                recon_pair<RECON>(v, theta, PL[q], PR[q]);
+            }
+            hydro_face_flux<RIEMANN, 1>(gamma, PL, PR, Fh);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) sm.Fy[q][fy][fx] = Fh[q];
+        }
+    }
+    __syncthreads();
+
+    // 3. divergence, RK combine, store
+    const float dt = at.dt();
+    float zdt = 3.0e38f;
+    // the rotation's three buffers are distinct arrays
+    const float* __restrict__ U0h = g.Uh[s];
+    const float* __restrict__ U0l = g.Ul[s];
+    const float* __restrict__ Uph = g.Uh[src];
+    const float* __restrict__ Upl = g.Ul[src];
+    float* __restrict__ Unh = g.Uh[dst];
+    float* __restrict__ Unl = g.Ul[dst];
+    const float idx = g.idx, idy = g.idy;
+    for (int c = threadIdx.x; c < TX * TY; c += NT) {
+        const int lx = c % TX, ly = c / TX;
+        const int x = tr.x0 + lx, y = tr.y0 + ly;
+        if (x >= n0 || y >= n1) continue;
+        const long long o = (long long) y * n0 + x;
+        float Unew[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            float L;
+            if constexpr (DIM == 2)
+                L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx, sm.Fy[q][ly][lx], sm.Fy[q][ly + 1][lx], idy);
+            else
+                L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx);
+            const df U0 = {ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
+            const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
+            const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
+            Unh[q * sU + o] = Un.hi;
+            Unl[q * sU + o] = Un.lo;
+            Unew[q] = Un.hi;
+        }
+        if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
+    }
+    if (last) block_min_to(at.cfl(), zdt);
+}
+
 // One RK stage over a list of tiles (persistent: CTAs stride over tiles).
-//   src: buffer holding the stage input; dst: buffer written; buffer 0 of a
-//   grid's rotation holds U0 (read per zone); b, omb = b, 1 - b.
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict__ grids,
                                                         const TileRef* __restrict__ tiles,
@@ -145,174 +459,19 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
                                                         int stage, float b, float omb, int last,
                                                         unsigned long long* __restrict__ cfl, int cfl_stride)
 {
-    constexpr int G = HaloOf<RECON>::G;
-    constexpr int WX = TX + 2 * G;
-    constexpr int WY = DIM == 2 ? TY + 2 * G : 1;
-    constexpr int FXN = (TX + 1) * TY;
-    constexpr int FYN = DIM == 2 ? TX * (TY + 1) : 1;
-    __shared__ float Ps[5][WY][WX];
-    __shared__ float Fx[5][TY][TX + 1];
-    __shared__ float Fy[5][DIM == 2 ? TY + 1 : 1][TX];
-
+    __shared__ TileSmem<DIM, RECON, TX, TY> sm;
     const int ntiles = *ntiles_p;  // device-resident so a captured graph follows a changing tile list
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const TileRef tr = tiles[t];
         const HGrid& g = grids[tr.grid];
         if (done[tr.grid * done_stride]) continue;
-        const int s = rot[tr.grid];
-        // buffer rotation: stage input / output per RK stage
-        int src, dst;
-        if (stage == 0) { src = s; dst = last ? (s ^ 1) : (s + 1) % 3; }
-        else if (stage == 1) { src = (s + 1) % 3; dst = last ? s : (s + 2) % 3; }
-        else { src = (s + 2) % 3; dst = s; }
-        const float* __restrict__ Uin = g.Uh[src];
-        const long long sU = g.sU;
-        const int n0 = g.n0, n1 = g.n1;
-
-        // L2 prefetch of what the update phase reads per zone besides the
-        // stage input's high word (already staged below): its low word and,
-        // after the first stage, both words of U0
-        {
-            const int rows = DIM == 2 ? TY : 1;
-            const int per = (TX * 4 + 127) / 128;            // 128-byte lines per row segment
-            const int arrays = stage == 0 ? 1 : 3;
-            const int lines = arrays * 5 * rows * per;
-            for (int l = threadIdx.x; l < lines; l += NT) {
-                const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
-                const int y = tr.y0 + r, x = tr.x0 + seg * 32;
-                if (y < n1 && x < n0) {
-                    const float* base = a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
-                    const float* ptr = base + q * sU + (long long) y * n0 + x;
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
-                }
-            }
-        }
-
-        __syncthreads(); // the previous tile's shared data is consumed
-        // 1. primitives of the tile and its halo: all loads first, then the
-        //    conversions, so each thread keeps NC x 5 loads in flight.  A tile
-        //    whose halo lies inside the grid reads it as one rectangle; the
-        //    others take every halo zone from its boundary image.
-        {
-            constexpr int NC = (WX * WY + NT - 1) / NT;
-            float Ur[NC][5];
-            int fl[NC];
-            const bool inner = tr.x0 - G >= 0 && tr.x0 + TX + G <= n0 &&
-                               (DIM == 1 || (tr.y0 - G >= 0 && tr.y0 + TY + G <= n1));
-            if (inner) {
-                const float* base = Uin + (long long) (tr.y0 - (DIM == 2 ? G : 0)) * n0 + (tr.x0 - G);
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                    const int c = threadIdx.x + k * NT;
-                    fl[k] = 0;
-                    if (c < WX * WY) {
-                        const int lx = c % WX, ly = c / WX;
-                        const float* p = base + (long long) ly * n0 + lx;
-#pragma unroll
-                        for (int q = 0; q < 5; ++q) Ur[k][q] = p[q * sU];
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                    const int c = threadIdx.x + k * NT;
-                    fl[k] = 0;
-                    if (c < WX * WY) {
-                        const int lx = c % WX, ly = c / WX;
-                        int flipx = 0, flipy = 0;
-                        const int x = bc_image(tr.x0 + lx - G, n0, g.bc, flipx);
-                        const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, n1, g.bc, flipy) : 0;
-                        const long long o = (long long) y * n0 + x;
-#pragma unroll
-                        for (int q = 0; q < 5; ++q) Ur[k][q] = Uin[q * sU + o];
-                        fl[k] = flipx | (flipy << 1);
-                    }
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                const int c = threadIdx.x + k * NT;
-                if (c < WX * WY) {
-                    const int lx = c % WX, ly = c / WX;
-                    if (fl[k] & 1) Ur[k][1] = -Ur[k][1];
-                    if (fl[k] & 2) Ur[k][2] = -Ur[k][2];
-                    float P[5];
-                    hydro_cons_f(g.gamma, Ur[k], P);
-#pragma unroll
-                    for (int q = 0; q < 5; ++q) Ps[q][ly][lx] = P[q];
-                }
-            }
-        }
-        __syncthreads();
-
-        const float theta = g.plm_theta, gamma = g.gamma;
-        // 2. x faces and y faces in one balanced loop (face fx sits left of
-        //    tile zone fx, face fy below tile row fy)
-        for (int f = threadIdx.x; f < FXN + (DIM == 2 ? FYN : 0); f += NT) {
-            float PL[5], PR[5], Fh[5];
-            if (f < FXN) {
-                const int fx = f % (TX + 1), fy = f / (TX + 1);
-                const int ry = DIM == 2 ? fy + G : 0;
-#pragma unroll
-                for (int q = 0; q < 5; ++q) {
-                    float v[2 * G];
-#pragma unroll
-                    for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][ry][fx + m];
-                    recon_pair<RECON>(v, theta, PL[q], PR[q]);
-                }
-                const float nx[3] = {1.f, 0.f, 0.f};
-                hydro_face_flux<RIEMANN>(gamma, PL, PR, nx, Fh);
-#pragma unroll
-                for (int q = 0; q < 5; ++q) Fx[q][fy][fx] = Fh[q];
-            } else if constexpr (DIM == 2) {
-                const int h = f - FXN;
-                const int fx = h % TX, fy = h / TX;
-#pragma unroll
-                for (int q = 0; q < 5; ++q) {
-                    float v[2 * G];
-#pragma unroll
-                    for (int m = 0; m < 2 * G; ++m) v[m] = Ps[q][fy + m][fx + G];
-                    recon_pair<RECON>(v, theta, PL[q], PR[q]);
-                }
-                const float ny[3] = {0.f, 1.f, 0.f};
-                hydro_face_flux<RIEMANN>(gamma, PL, PR, ny, Fh);
-#pragma unroll
-                for (int q = 0; q < 5; ++q) Fy[q][fy][fx] = Fh[q];
-            }
-        }
-        __syncthreads();
-
-        // 3. divergence, RK combine, store
-        const float dt = (float) dtg[tr.grid * dt_stride];
-        float zdt = 3.0e38f;
-        // the rotation's three buffers are distinct arrays
-        const float* __restrict__ U0h = g.Uh[s];
-        const float* __restrict__ U0l = g.Ul[s];
-        const float* __restrict__ Uph = g.Uh[src];
-        const float* __restrict__ Upl = g.Ul[src];
-        float* __restrict__ Unh = g.Uh[dst];
-        float* __restrict__ Unl = g.Ul[dst];
-        const float idx = g.idx, idy = g.idy;
-        for (int c = threadIdx.x; c < TX * TY; c += NT) {
-            const int lx = c % TX, ly = c / TX;
-            const int x = tr.x0 + lx, y = tr.y0 + ly;
-            if (x >= n0 || y >= n1) continue;
-            const long long o = (long long) y * n0 + x;
-            float Unew[5];
-#pragma unroll
-            for (int q = 0; q < 5; ++q) {
-                float L = -(Fx[q][ly][lx + 1] - Fx[q][ly][lx]) * idx;
-                if constexpr (DIM == 2) L -= (Fy[q][ly + 1][lx] - Fy[q][ly][lx]) * idy;
-                const df U0 = {U0h[q * sU + o], U0l[q * sU + o]};
-                const df Up = {Uph[q * sU + o], Upl[q * sU + o]};
-                const df Un = rk_combine(U0, Up, dt * L, b, omb);
-                Unh[q * sU + o] = Un.hi;
-                Unl[q * sU + o] = Un.lo;
-                Unew[q] = Un.hi;
-            }
-            if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
-        }
-        if (last) block_min_to(&cfl[tr.grid * cfl_stride], zdt);
+        struct {
+            const double* dtp;
+            unsigned long long* slot;
+            __device__ float dt() const { return (float) *dtp; }
+            __device__ unsigned long long* cfl() const { return slot; }
+        } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride};
+        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
     }
 }
 

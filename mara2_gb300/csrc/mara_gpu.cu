@@ -663,6 +663,18 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
 
 int mara_gpu_advance_host(MaraGpuHandle* h, double* P_aos, double t0, double dt)
 {
+    if (h && P_aos && h->mixed && !h->timing && mixed_host_step_capable(h->mixed)) {
+        if (double* d = (double*) direct_host_pointer(P_aos)) {
+            // page-locked host array: transfers and stages pipelined in one launch
+            CK(cudaSetDevice(h->cfg.device));
+            k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+            h->launches++;
+            const int rc = mixed_advance_host_step(h->mixed, d, dt, h->st, h->stream, &h->launches);
+            if (rc) return rc;
+            h->steps++;
+            return read_status(h);
+        }
+    }
     int rc = mara_gpu_upload(h, P_aos);
     if (!rc) rc = mara_gpu_advance(h, t0, dt);
     if (!rc) rc = mara_gpu_download(h, P_aos);

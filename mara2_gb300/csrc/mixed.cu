@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restri
 
 // FP64 primitives of cell c (AoS order) from the FP32-pair state; a guard
 // zone is the boundary image of an interior zone
-template <int LAW>
+template <int LAW, bool L2ONLY = false>
 __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, long long c, const GridF& G,
                                            const PhysParams& pp, double* out)
 {
@@ -381,7 +381,8 @@ __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, lon
     const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
     double U[NQ], P[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) U[q] = (double) Uh[q * G.sU + u] + (double) Ul[q * G.sU + u];
+    for (int q = 0; q < NQ; ++q)
+        U[q] = (double) ld_state<L2ONLY>(Uh + q * G.sU + u) + (double) ld_state<L2ONLY>(Ul + q * G.sU + u);
     if constexpr (LAW == LAW_HYDRO) {
         hydro_u2p_d(U, G.gm1_d, P);
     } else {
@@ -470,7 +471,10 @@ struct MixedState {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
     double ms = 0;
     int64_t nlaunch = 0;
+    struct HostStep* hs = nullptr;   // the pipelined host step (created on first use)
 };
+
+static void host_step_destroy(HostStep* hs);
 
 static int dev_alloc(void** p, size_t bytes, cudaStream_t s, int64_t* total)
 {
@@ -571,6 +575,7 @@ void mixed_destroy(MixedState* m)
     cudaFree(m->dgrid);
     cudaFree(m->dtiles);
     cudaFree(m->dntiles);
+    host_step_destroy(m->hs);
     delete m;
 }
 
@@ -830,6 +835,441 @@ bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t
     fused_step(m, &st->dt, st, s);
     if (m->cfg.rk_order == 1) m->rot ^= 1;
     return true;
+}
+
+// ---- the host step: transfers and stages in one pipelined launch ----------------
+// MethodOfLinesTVD::advance on a page-locked host MeshData::P (FP64 AoS, i
+// the slowest index: a host row is one column of zones) as one launch whose
+// CTAs take items from two ordered queues:
+//   IN     one interior host row -> FP32-pair state (read over the chip-to-chip link);
+//   WORK   STAGE: one RK stage of one 32 x 16 tile, or
+//          OUT: one host row (interior or guard) <- FP32-pair state (written over the link).
+// A stage-0 tile needs the IN rows its stencil reads, a later stage the
+// previous stage of the 3 x 3 tiles around it, an OUT row the last stage of
+// its tile column (a guard row: of the first and the last column).  The
+// first in_ctas CTAs take IN rows (they never wait) and then join the
+// others, which take WORK items in queue order and wait for the completion
+// flags of what each needs.  The WORK queue lists every item after all it
+// needs, so the earliest unfinished WORK item has its inputs complete or
+// being loaded, and every wait ends.  Both queues take the tile columns in
+// transfer order (with periodic boundaries the last column first: it is the
+// first one's left neighbour), so transfers in, stages and transfers out
+// overlap.  CTAs read the state that other CTAs wrote from L2
+// (ld.global.cg).  The per-zone arithmetic is that of load_kernel,
+// hydro_tile_kernel and store_kernel.
+enum { HS_IN = 0, HS_STAGE = 1, HS_OUT = 4 };  // item kinds: IN, stages 0..2, OUT
+constexpr int HS_SLAB = 512;               // cells staged in shared memory at a time
+constexpr int HS_POLLS = 1 << 22;          // about a second of waiting, then an error
+constexpr int HS_LAG = 256;                // WORK items listed between a stage tile and its readers
+
+__host__ __device__ constexpr int hs_item(int kind, int idx) { return (kind << 26) | idx; }
+
+struct HostStepJob {
+    const HGrid* grid;
+    double* host;            // device address of the page-locked host array
+    const int* in_q;         // IN rows in transfer order
+    const int* work_q;       // WORK items (hs_item codes)
+    int n_in, n_work;
+    int in_ctas;
+    int* head;               // [0] IN, [1] WORK, [2] error; zero at launch
+    int* in_flag;            // per interior host row, the epoch once loaded
+    int* tile_flag;          // per stage and tile, the epoch once written
+    DevStatus* st;
+    const TileRef* tiles;    // row-major: t = ty * ntx + tx
+    int ntx, nty;            // tiles per row / column
+    int n0, g0, halo;        // interior and guard host rows, stencil half-width
+    long long row;           // cells per host row
+    int periodic;
+    int r, order;            // the state's buffer, RK order
+    float bst[3];
+    double dt;
+    unsigned long long* cfl;
+    int epoch;
+    GridF G;
+};
+
+// the interior row / tile a stencil coordinate reads (periodic wrap), or -1
+__device__ __forceinline__ int hs_wrap(int x, int n, int periodic)
+{
+    if (x >= 0 && x < n) return x;
+    if (periodic) return (x + n) % n;
+    return -1;
+}
+
+// wait until flag *f holds the epoch (bounded; a timeout sets the error,
+// which ends every wait and the launch)
+__device__ __forceinline__ void hs_wait_flag(const HostStepJob& J, const int* f)
+{
+    int polls = 0;
+    while (*(volatile const int*) f != J.epoch) {
+        if (*(volatile int*) &J.head[2]) return;
+        if (++polls > HS_POLLS) {
+            if (atomicExch(&J.head[2], 1) == 0) atomicCAS(&J.st->code, 0, MARA_ERR_CUDA);
+            return;
+        }
+        __nanosleep(polls < 32 ? 64 : 512);
+    }
+}
+
+// one warp: wait for every input of WORK item (kind, idx)
+__device__ __forceinline__ void hs_wait_inputs(const HostStepJob& J, int kind, int idx)
+{
+    const int lane = threadIdx.x & 31;
+    if (kind == HS_STAGE) {
+        const int tx = idx % J.ntx;
+        const int x0 = tx * 32 - J.halo, w = min(32, J.n0 - tx * 32) + 2 * J.halo;
+        for (int i = lane; i < w; i += 32) {
+            const int x = hs_wrap(x0 + i, J.n0, J.periodic);
+            if (x >= 0) hs_wait_flag(J, &J.in_flag[x]);
+        }
+    } else if (kind < HS_OUT) {
+        const int tx = idx % J.ntx, ty = idx / J.ntx;
+        const int* f = J.tile_flag + (kind - HS_STAGE - 1) * J.ntx * J.nty;
+        if (lane < 9) {
+            const int x = hs_wrap(tx + lane % 3 - 1, J.ntx, J.periodic);
+            const int y = hs_wrap(ty + lane / 3 - 1, J.nty, J.periodic);
+            if (x >= 0 && y >= 0) hs_wait_flag(J, &f[y * J.ntx + x]);
+        }
+    } else {
+        const int* f = J.tile_flag + (J.order - 1) * J.ntx * J.nty;
+        const int cols = idx < J.n0 ? 1 : 2;  // a guard row: the first and the last column
+        for (int i = lane; i < cols * J.nty; i += 32) {
+            const int tx = idx < J.n0 ? idx / 32 : (i < J.nty ? 0 : J.ntx - 1);
+            hs_wait_flag(J, &f[(i % J.nty) * J.ntx + tx]);
+        }
+    }
+    __syncwarp();
+}
+
+template <int RECON, int RIEMANN>
+__global__ void __launch_bounds__(256, 4) host_step_kernel(const __grid_constant__ HostStepJob J)
+{
+    union Smem {
+        TileSmem<2, RECON, 32, 16> t;
+        double slab[HS_SLAB * 5];
+    };
+    __shared__ Smem sm;
+    __shared__ int got_k, got_idx;
+    const HGrid& g = *J.grid;
+    bool in_role = blockIdx.x < J.in_ctas;  // read and written by thread 0 only
+    for (;;) {
+        __syncthreads();  // the previous item's shared data is consumed
+        // 1. the next IN row (the first in_ctas CTAs, while rows are left),
+        //    else the next WORK item and, for warp 0, the wait for its inputs
+        if (threadIdx.x < 32) {
+            int k = -2, idx = 0;
+            if (threadIdx.x == 0) {
+                if (in_role) {
+                    const int h = atomicAdd(&J.head[0], 1);
+                    if (h < J.n_in) { k = HS_IN; idx = J.in_q[h]; }
+                    else in_role = false;
+                }
+                if (!in_role) {
+                    const int h = atomicAdd(&J.head[1], 1);
+                    if (h < J.n_work) { const int c = J.work_q[h]; k = c >> 26; idx = c & ((1 << 26) - 1); }
+                }
+            }
+            k = __shfl_sync(0xffffffffu, k, 0);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            if (k > HS_IN) hs_wait_inputs(J, k, idx);
+            __threadfence();
+            if (threadIdx.x == 0) { got_k = k; got_idx = idx; }
+        }
+        __syncthreads();
+        const int kind = got_k, idx = got_idx;
+        if (kind < 0) return;
+        // 2. the work
+        if (kind >= HS_STAGE && kind < HS_OUT) {
+            const int stage = kind - HS_STAGE;
+            const int last = stage == J.order - 1;
+            const float b = J.bst[stage];
+            struct {
+                const HostStepJob* j;
+                __device__ float dt() const { return (float) j->dt; }
+                __device__ unsigned long long* cfl() const { return j->cfl; }
+            } at{&J};
+            tile_stage<2, RECON, RIEMANN, 32, 16, 256, true>(sm.t, g, J.tiles[idx], J.r, stage, b, 1.f - b, last, at);
+        } else {
+            // host row i: interior row idx, or a guard row after the interior ones
+            const int i = kind == HS_IN || idx < J.n0 ? J.g0 + idx
+                          : idx < J.n0 + J.g0 ? idx - J.n0 : J.g0 + J.n0 + (idx - J.n0 - J.g0);
+            const long long c0 = (long long) i * J.row, c1 = c0 + J.row;
+            const int out_buf = J.order == 1 ? J.r ^ 1 : J.r;
+            for (long long b0 = c0; b0 < c1; b0 += HS_SLAB) {
+                const int nc = (int) min((long long) HS_SLAB, c1 - b0);
+                if (kind == HS_IN) {
+                    // every load in flight before the first use
+                    constexpr int PER = HS_SLAB * 5 / 256;
+                    double v[PER];
+#pragma unroll
+                    for (int u = 0; u < PER; ++u) {
+                        const int e = threadIdx.x + u * 256;
+                        v[u] = e < nc * 5 ? J.host[b0 * 5 + e] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < PER; ++u) sm.slab[threadIdx.x + u * 256] = v[u];
+                    __syncthreads();
+                    const GridF& G = J.G;
+                    for (int cc = threadIdx.x; cc < nc; cc += 256) {
+                        const int jj = (int) ((b0 + cc) % G.N[1]) - G.g[1];
+                        if (jj < 0 || jj >= G.n[1]) continue;
+                        double P[5], U[5];
+#pragma unroll
+                        for (int q = 0; q < 5; ++q) P[q] = sm.slab[cc * 5 + q];
+                        hydro_p2u_d(P, G.inv_gm1_d, U);
+                        const long long u = (long long) jj * G.n[0] + idx;
+#pragma unroll
+                        for (int q = 0; q < 5; ++q) {
+                            const df d = df_from_double(U[q]);
+                            g.Uh[J.r][q * G.sU + u] = d.hi;
+                            g.Ul[J.r][q * G.sU + u] = d.lo;
+                        }
+                    }
+                } else {
+                    for (int cc = threadIdx.x; cc < nc; cc += 256)
+                        store_cell<LAW_HYDRO, true>(g.Uh[out_buf], g.Ul[out_buf], b0 + cc, J.G, PhysParams(),
+                                                    &sm.slab[cc * 5]);
+                    __syncthreads();
+                    for (int e = threadIdx.x; e < nc * 5; e += 256) J.host[b0 * 5 + e] = sm.slab[e];
+                }
+                __syncthreads();
+            }
+        }
+        // 3. publish
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (kind == HS_IN) *(volatile int*) &J.in_flag[idx] = J.epoch;
+            else if (kind < HS_OUT) *(volatile int*) &J.tile_flag[(kind - HS_STAGE) * J.ntx * J.nty + idx] = J.epoch;
+        }
+    }
+}
+
+__global__ void k_host_step_begin(DevStatus* st, unsigned long long* cfl, int* head, int* drot, int rot_after,
+                                  double dt)
+{
+    st->dt = dt;
+    *cfl = (unsigned long long) __double_as_longlong(DBL_MAX);
+    for (int k = 0; k < 4; ++k) head[k] = 0;
+    *drot = rot_after;
+}
+
+struct HostStep {
+    int ntx = 0, nty = 0;
+    int* dq = nullptr;        // the IN queue, then the WORK queue
+    int n_in = 0, n_work = 0;
+    int* dhead = nullptr;
+    int* dflags = nullptr;    // IN row flags, then the stages' tile flags
+    size_t nflags = 0;
+    int epoch = 0;
+    int grid = 0;             // CTAs of the launch
+    int in_ctas = 0;
+};
+
+static void host_step_destroy(HostStep* hs)
+{
+    if (!hs) return;
+    cudaFree(hs->dq);
+    cudaFree(hs->dhead);
+    cudaFree(hs->dflags);
+    delete hs;
+}
+
+bool mixed_host_step_capable(const MixedState* m)
+{
+    // a stage reads one tile either side only if the last tile row and column
+    // hold at least the two-zone halo
+    const int rx = m->G.n[0] % 32, ry = m->G.n[1] % 16;
+    return m->fused && m->G.n[1] > 1 && m->G.N[2] == 1 && m->G.n[0] >= 128 && m->tx == 32 && m->ty == 16 &&
+           (rx == 0 || rx >= 2) && (ry == 0 || ry >= 2);
+}
+
+template <int RECON, int RIEMANN>
+static int host_step_occupancy()
+{
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, host_step_kernel<RECON, RIEMANN>, 256, 0) != cudaSuccess)
+        return 0;
+    return per;
+}
+
+// The queues.  Tile columns in transfer order; IN lists their rows; WORK
+// lists, after each column's rows, every stage tile whose inputs are now
+// listed, stage by stage, then the OUT rows of every column whose last stage
+// is; the guard rows come last.  A stage tile or an OUT row is listed only
+// HS_LAG items after the stage tiles it reads, so that they are usually
+// complete when a CTA takes it (a CTA waiting for inputs holds its slot);
+// when nothing else can be listed the lag is dropped.
+static void host_step_queues(int n0, int ntx, int nty, int order, bool periodic, int g0, std::vector<int>& in_q,
+                             std::vector<int>& work_q)
+{
+    std::vector<char> in(ntx, 0), out(ntx, 0);
+    // per stage and tile: -1 until listed, then its WORK position
+    std::vector<std::vector<int>> st(order, std::vector<int>((size_t) ntx * nty, -1));
+    std::vector<int> last_pos(ntx, -1), cnt_last(ntx, 0);
+    auto wrap = [&](int x, int n, bool& ok) {
+        ok = true;
+        if (x >= 0 && x < n) return x;
+        if (periodic) return (x + n) % n;
+        ok = false;
+        return 0;
+    };
+    // list everything whose inputs were listed at least `lag` items before
+    auto sweep = [&](int lag) {
+        bool any = false;
+        for (bool more = true; more;) {
+            more = false;
+            const int now = (int) work_q.size();
+            for (int k = 0; k < order; ++k)
+                for (int tx = 0; tx < ntx; ++tx)
+                    for (int ty = 0; ty < nty; ++ty) {
+                        const int t = ty * ntx + tx;
+                        if (st[k][t] >= 0) continue;
+                        bool ready = true;
+                        if (k == 0) {
+                            for (int d = -1; d <= 1 && ready; ++d) {
+                                bool ok;
+                                const int x = wrap(tx + d, ntx, ok);
+                                if (ok) ready = in[x];
+                            }
+                        } else {
+                            for (int dy = -1; dy <= 1 && ready; ++dy)
+                                for (int dx = -1; dx <= 1 && ready; ++dx) {
+                                    bool okx, oky;
+                                    const int x = wrap(tx + dx, ntx, okx), y = wrap(ty + dy, nty, oky);
+                                    if (okx && oky) {
+                                        const int p = st[k - 1][y * ntx + x];
+                                        ready = p >= 0 && p + lag <= now;
+                                    }
+                                }
+                        }
+                        if (!ready) continue;
+                        st[k][t] = (int) work_q.size();
+                        work_q.push_back(hs_item(HS_STAGE + k, t));
+                        if (k == order - 1) {
+                            cnt_last[tx]++;
+                            last_pos[tx] = st[k][t];
+                        }
+                        more = any = true;
+                    }
+            for (int tx = 0; tx < ntx; ++tx)
+                if (!out[tx] && cnt_last[tx] == nty && last_pos[tx] + lag <= now) {
+                    for (int x = tx * 32; x < std::min(n0, tx * 32 + 32); ++x) work_q.push_back(hs_item(HS_OUT, x));
+                    out[tx] = 1;
+                    more = any = true;
+                }
+        }
+        return any;
+    };
+    std::vector<int> cols;
+    if (periodic) cols.push_back(ntx - 1);
+    for (int b = 0; b < ntx; ++b) if (!(periodic && b == ntx - 1)) cols.push_back(b);
+    for (int b : cols) {
+        for (int x = b * 32; x < std::min(n0, b * 32 + 32); ++x) in_q.push_back(x);
+        in[b] = 1;
+        sweep(HS_LAG);
+    }
+    while (sweep(HS_LAG) || sweep(0)) {
+    }
+    for (int k = 0; k < 2 * g0; ++k) work_q.push_back(hs_item(HS_OUT, n0 + k));
+}
+
+static int host_step_setup(MixedState* m)
+{
+    HostStep* hs = new HostStep();
+    m->hs = hs;
+    const int order = m->cfg.rk_order;
+    hs->ntx = (m->G.n[0] + 31) / 32;
+    hs->nty = (m->G.n[1] + 15) / 16;
+    std::vector<int> in_q, work_q;
+    host_step_queues(m->G.n[0], hs->ntx, hs->nty, order, m->G.bc == BC_PERIODIC, m->G.g[0], in_q, work_q);
+    hs->n_in = (int) in_q.size();
+    hs->n_work = (int) work_q.size();
+    std::vector<int> all(in_q);
+    all.insert(all.end(), work_q.begin(), work_q.end());
+    hs->nflags = (size_t) m->G.n[0] + (size_t) order * hs->ntx * hs->nty;
+    if (cudaMalloc((void**) &hs->dq, sizeof(int) * all.size()) != cudaSuccess ||
+        cudaMalloc((void**) &hs->dhead, sizeof(int) * 4) != cudaSuccess ||
+        cudaMalloc((void**) &hs->dflags, sizeof(int) * hs->nflags) != cudaSuccess)
+        return MARA_ERR_CUDA;
+    if (cudaMemcpy(hs->dq, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(hs->dflags, 0, sizeof(int) * hs->nflags) != cudaSuccess)
+        return MARA_ERR_CUDA;
+    int per = 0, dev = 0, sms = 0;
+    const bool hllc = m->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (m->cfg.recon == MARA_RECON_PCM)
+        per = hllc ? host_step_occupancy<RECON_PCM, RIEMANN_HLLC>() : host_step_occupancy<RECON_PCM, RIEMANN_HLLE>();
+    else
+        per = hllc ? host_step_occupancy<RECON_PLM, RIEMANN_HLLC>() : host_step_occupancy<RECON_PLM, RIEMANN_HLLE>();
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (per < 2) return MARA_ERR_CUDA;
+    hs->grid = per * sms;
+    hs->in_ctas = sms;  // one loading CTA per SM keeps the link busy
+    return MARA_OK;
+}
+
+template <int RECON, int RIEMANN>
+static cudaError_t host_step_launch(const HostStepJob& J, int grid, cudaStream_t s)
+{
+    void* args[] = {(void*) &J};
+    return cudaLaunchCooperativeKernel((const void*) host_step_kernel<RECON, RIEMANN>, dim3(grid), dim3(256), args, 0,
+                                       s);
+}
+
+int mixed_advance_host_step(MixedState* m, double* host_dev, double dt, DevStatus* st, cudaStream_t s,
+                            int64_t* launches)
+{
+    if (!m->hs) {
+        const int rc = host_step_setup(m);
+        if (rc) { host_step_destroy(m->hs); m->hs = nullptr; return rc; }
+    }
+    HostStep* hs = m->hs;
+    const int order = m->cfg.rk_order;
+    const int r = host_rot(m);
+    const int rot_after = order == 1 ? r ^ 1 : r;
+    hs->epoch = hs->epoch == 0x3fffffff ? 1 : hs->epoch + 1;
+    if (hs->epoch == 1) cudaMemsetAsync(hs->dflags, 0, sizeof(int) * hs->nflags, s);
+    k_host_step_begin<<<1, 1, 0, s>>>(st, m->dcfl, hs->dhead, m->drot, rot_after, dt);
+    HostStepJob J = {};
+    J.grid = m->dgrid;
+    J.host = host_dev;
+    J.in_q = hs->dq;
+    J.work_q = hs->dq + hs->n_in;
+    J.n_in = hs->n_in;
+    J.n_work = hs->n_work;
+    J.in_ctas = hs->in_ctas;
+    J.head = hs->dhead;
+    J.in_flag = hs->dflags;
+    J.tile_flag = hs->dflags + m->G.n[0];
+    J.st = st;
+    J.tiles = m->dtiles;
+    J.ntx = hs->ntx;
+    J.nty = hs->nty;
+    J.n0 = m->G.n[0];
+    J.g0 = m->G.g[0];
+    J.halo = m->cfg.recon == MARA_RECON_PCM ? 1 : 2;
+    J.row = (long long) m->G.N[1] * m->G.N[2];
+    J.periodic = m->G.bc == BC_PERIODIC;
+    J.r = r;
+    J.order = order;
+    for (int k = 0; k < 3; ++k) J.bst[k] = B_TAB[order - 1][k];
+    J.dt = dt;
+    J.cfl = m->dcfl;
+    J.epoch = hs->epoch;
+    J.G = m->GF;
+    cudaError_t e;
+    const bool hllc = m->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (m->cfg.recon == MARA_RECON_PCM)
+        e = hllc ? host_step_launch<RECON_PCM, RIEMANN_HLLC>(J, hs->grid, s)
+                 : host_step_launch<RECON_PCM, RIEMANN_HLLE>(J, hs->grid, s);
+    else
+        e = hllc ? host_step_launch<RECON_PLM, RIEMANN_HLLC>(J, hs->grid, s)
+                 : host_step_launch<RECON_PLM, RIEMANN_HLLE>(J, hs->grid, s);
+    if (e != cudaSuccess) return MARA_ERR_CUDA;
+    *launches += 2;
+    m->rot = rot_after;
+    return MARA_OK;
 }
 
 int mixed_launches_per_step(const MixedState* m)

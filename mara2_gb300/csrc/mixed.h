@@ -25,6 +25,12 @@ void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);
 // enqueued) otherwise.
 bool mixed_enqueue_run_step(MixedState* m, double cfl, double t_final, DevStatus* st, cudaStream_t s);
 bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t s);
+// one advance of a page-locked host MeshData::P in place (host_dev: its
+// device address), the transfers and the stages pipelined in one launch
+// (2-D fused grids)
+bool mixed_host_step_capable(const MixedState* m);
+int mixed_advance_host_step(MixedState* m, double* host_dev, double dt, DevStatus* st, cudaStream_t s,
+                            int64_t* launches);
 int mixed_launches_per_step(const MixedState* m);
 bool mixed_fused(const MixedState* m);
 // 1-D hydro grids of up to 8192 zones on the fused form: up to nsteps

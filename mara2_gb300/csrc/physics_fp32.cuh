@@ -23,36 +23,38 @@ struct df {
     float hi, lo;
 };
 
+// every operation explicitly rounded: no multiply-add contraction can break
+// the error-free transformations, and every kernel computes the same bits
 __device__ __forceinline__ df two_sum(float a, float b)
 {
-    const float s = a + b;
-    const float bb = s - a;
-    const float e = (a - (s - bb)) + (b - bb);
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
     return {s, e};
 }
 
 __device__ __forceinline__ df fast_two_sum(float a, float b)
 {
-    const float s = a + b;
-    const float e = b - (s - a);
+    const float s = __fadd_rn(a, b);
+    const float e = __fsub_rn(b, __fsub_rn(s, a));
     return {s, e};
 }
 
 __device__ __forceinline__ df df_add_f(df a, float b)
 {
     df s = two_sum(a.hi, b);
-    return fast_two_sum(s.hi, s.lo + a.lo);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 
 __device__ __forceinline__ df df_add(df a, df b)
 {
     df s = two_sum(a.hi, b.hi);
-    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
 __device__ __forceinline__ df df_mul_f(df a, float b)
 {
-    const float p = a.hi * b;
+    const float p = __fmul_rn(a.hi, b);
     float e = __fmaf_rn(a.hi, b, -p);
     e = __fmaf_rn(a.lo, b, e);
     return fast_two_sum(p, e);
@@ -75,7 +77,7 @@ __device__ __forceinline__ df rk_combine(df U0, df U, float dtL, float b, float 
     if (one_minus_b == 0.0f) return s;
     if (b == 0.5f) {  // (U0 + s) / 2: halving is exact on both words
         const df t = df_add(U0, s);
-        return {0.5f * t.hi, 0.5f * t.lo};
+        return {__fmul_rn(0.5f, t.hi), __fmul_rn(0.5f, t.lo)};
     }
     return df_add(df_mul_f(U0, one_minus_b), df_mul_f(s, b));
 }

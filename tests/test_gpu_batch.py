@@ -9,7 +9,6 @@ import dataclasses
 import numpy as np
 import pytest
 
-from helpers import rel_l1
 from mara2_gb300 import workloads as W
 
 
@@ -64,10 +63,7 @@ def _run_batch(built, **kw):
 def test_cluster_slots_match_lockstep(gpu_lib):
     """1-D grids of every cluster class (1 to 8 CTAs, up to 1024 zones per
     CTA) run on their own clusters beside 2-D grids in the tile lists, against
-    all grids stepping in lockstep: the 2-D grids give the same bits, the 1-D
-    grids the same clock and step count and states equal to FP32 rounding
-    (the cluster kernel is a separately compiled FP32 kernel, whose multiply-
-    adds the compiler may fuse differently)."""
+    all grids stepping in lockstep: the same clock, step count and bits."""
     reqs = W.riemann_stream(40, rate=1e6, seed=5, n1=(64, 512), n2=(32, 64))
     one = [r for r in reqs if r.dims == 1][:6]
     two = [r for r in reqs if r.dims == 2][:4]
@@ -82,12 +78,8 @@ def test_cluster_slots_match_lockstep(gpu_lib):
     for k, (s, _) in enumerate(built):
         Pa, ta, na = a[k]
         Pb, tb, nb = b[k]
-        assert na == nb and abs(ta - tb) <= 1e-12 * tb, (k, na, nb, ta, tb)
-        if s.shape[1] > 1:
-            assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), k
-        else:
-            err = rel_l1(Pa[s.interior()], Pb[s.interior()])
-            assert err[0] < 1e-6 and err[4] < 1e-6, (k, err)
+        assert na == nb and ta == tb, (k, na, nb, ta, tb)
+        assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), k
 
 
 @pytest.mark.gpu
