@@ -670,9 +670,12 @@ int mara_gpu_advance_host(MaraGpuHandle* h, double* P_aos, double t0, double dt)
             k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
             h->launches++;
             const int rc = mixed_advance_host_step(h->mixed, d, dt, h->st, h->stream, &h->launches);
-            if (rc) return rc;
-            h->steps++;
-            return read_status(h);
+            if (rc != MIXED_NOT_TAKEN) {
+                if (rc) return rc;
+                h->steps++;
+                return read_status(h);
+            }
+            // not available on this device: the unpipelined path below
         }
     }
     int rc = mara_gpu_upload(h, P_aos);

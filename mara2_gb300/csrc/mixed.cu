@@ -472,6 +472,7 @@ struct MixedState {
     double ms = 0;
     int64_t nlaunch = 0;
     struct HostStep* hs = nullptr;   // the pipelined host step (created on first use)
+    bool hs_unavailable = false;     // it could not be set up or launched here
 };
 
 static void host_step_destroy(HostStep* hs);
@@ -951,7 +952,9 @@ __global__ void __launch_bounds__(256, 4) host_step_kernel(const __grid_constant
     __shared__ Smem sm;
     __shared__ int got_k, got_idx;
     const HGrid& g = *J.grid;
-    bool in_role = blockIdx.x < J.in_ctas;  // read and written by thread 0 only
+    // CTAs 0 .. in_ctas - 1 load, one per SM (a cooperative launch: every CTA
+    // is resident, so a WORK item's IN rows are always being taken); thread 0's
+    bool in_role = blockIdx.x < J.in_ctas;
     for (;;) {
         __syncthreads();  // the previous item's shared data is consumed
         // 1. the next IN row (the first in_ctas CTAs, while rows are left),
@@ -1050,7 +1053,7 @@ __global__ void k_host_step_begin(DevStatus* st, unsigned long long* cfl, int* h
 {
     st->dt = dt;
     *cfl = (unsigned long long) __double_as_longlong(DBL_MAX);
-    for (int k = 0; k < 4; ++k) head[k] = 0;
+    for (int k = 0; k < 8; ++k) head[k] = 0;
     *drot = rot_after;
 }
 
@@ -1189,7 +1192,7 @@ static int host_step_setup(MixedState* m)
     all.insert(all.end(), work_q.begin(), work_q.end());
     hs->nflags = (size_t) m->G.n[0] + (size_t) order * hs->ntx * hs->nty;
     if (cudaMalloc((void**) &hs->dq, sizeof(int) * all.size()) != cudaSuccess ||
-        cudaMalloc((void**) &hs->dhead, sizeof(int) * 4) != cudaSuccess ||
+        cudaMalloc((void**) &hs->dhead, sizeof(int) * 8) != cudaSuccess ||
         cudaMalloc((void**) &hs->dflags, sizeof(int) * hs->nflags) != cudaSuccess)
         return MARA_ERR_CUDA;
     if (cudaMemcpy(hs->dq, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1220,9 +1223,15 @@ static cudaError_t host_step_launch(const HostStepJob& J, int grid, cudaStream_t
 int mixed_advance_host_step(MixedState* m, double* host_dev, double dt, DevStatus* st, cudaStream_t s,
                             int64_t* launches)
 {
+    if (m->hs_unavailable) return MIXED_NOT_TAKEN;
     if (!m->hs) {
-        const int rc = host_step_setup(m);
-        if (rc) { host_step_destroy(m->hs); m->hs = nullptr; return rc; }
+        if (host_step_setup(m)) {
+            host_step_destroy(m->hs);
+            m->hs = nullptr;
+            m->hs_unavailable = true;
+            cudaGetLastError();
+            return MIXED_NOT_TAKEN;
+        }
     }
     HostStep* hs = m->hs;
     const int order = m->cfg.rk_order;
@@ -1266,7 +1275,12 @@ int mixed_advance_host_step(MixedState* m, double* host_dev, double dt, DevStatu
     else
         e = hllc ? host_step_launch<RECON_PLM, RIEMANN_HLLC>(J, hs->grid, s)
                  : host_step_launch<RECON_PLM, RIEMANN_HLLE>(J, hs->grid, s);
-    if (e != cudaSuccess) return MARA_ERR_CUDA;
+    if (e != cudaSuccess) {
+        // a cooperative launch this device cannot run: the unpipelined path
+        cudaGetLastError();
+        m->hs_unavailable = true;
+        return MIXED_NOT_TAKEN;
+    }
     *launches += 2;
     m->rot = rot_after;
     return MARA_OK;

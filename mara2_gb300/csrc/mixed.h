@@ -28,6 +28,9 @@ bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t
 // one advance of a page-locked host MeshData::P in place (host_dev: its
 // device address), the transfers and the stages pipelined in one launch
 // (2-D fused grids)
+// MIXED_NOT_TAKEN: the pipelined step cannot run on this device (it then
+// stays off for the handle); nothing was changed, use the unpipelined path
+constexpr int MIXED_NOT_TAKEN = -1;
 bool mixed_host_step_capable(const MixedState* m);
 int mixed_advance_host_step(MixedState* m, double* host_dev, double dt, DevStatus* st, cudaStream_t s,
                             int64_t* launches);
