@@ -249,9 +249,12 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
     float Pn[NQ];
     int code = ST_OK;
     const long long pc = ((long long) k * G.N[1] + j) * G.N[0] + i;
+    // the zone's previous primitives: the RMHD recovery's starting point, and
+    // what a failed recovery keeps (read only then for the other laws)
     float Pold[NQ];
+    if constexpr (LAW == LAW_RMHD)
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) Pold[q] = Pf[q * G.sP + pc];
+        for (int q = 0; q < NQ; ++q) Pold[q] = Pf[q * G.sP + pc];
     const int e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
     if (e == ST_INVERSION_FAILURE) {
         atomicAdd(&st->failures, 1);
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
         const unsigned long long prev = atomicMin(&st->first_zone, z);
         if (z < prev) atomicExch(&st->first_code, code);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Pn[q] = Pold[q];
+        for (int q = 0; q < NQ; ++q) Pn[q] = LAW == LAW_RMHD ? Pold[q] : Pf[q * G.sP + pc];
     }
     int ix[4], iy[4], iz[4], sx[4], sy[4], sz[4];
     const int cx = guard_images_m(ii, G.n[0], G.g[0], G.bc, ix, sx);
