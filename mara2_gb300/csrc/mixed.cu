@@ -134,22 +134,30 @@ __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G,
     return V.at(a, q, i, j, k);
 }
 
-__device__ __forceinline__ int guard_images_m(int ii, int n, int g, int bc, int* out, int* flip)
+// image number idx of interior coordinate ii on one axis, or false where
+// there is none: 0 is the zone's own cell, then the guard cells that hold its
+// image (periodic: the copy across the grid; outflow: the whole guard layer
+// beside an edge zone; reflecting: the mirror cell, whose normal momentum
+// flips), as BoundaryCondition::applySimple fills them
+__device__ __forceinline__ bool guard_image_m(int idx, int ii, int n, int g, int bc, int& o, int& f)
 {
-    int c = 0;
-    out[c] = ii + g; flip[c] = 0; ++c;
-    if (g == 0) return c;
+    f = 0;
+    if (idx == 0) { o = ii + g; return true; }
+    if (g == 0) return false;
+    int c = 1;
     if (bc == BC_PERIODIC) {
-        if (ii < g) { out[c] = ii + g + n; flip[c] = 0; ++c; }
-        if (ii >= n - g) { out[c] = ii + g - n; flip[c] = 0; ++c; }
+        if (ii < g) { if (idx == c) { o = ii + g + n; return true; } ++c; }
+        if (ii >= n - g) { if (idx == c) { o = ii + g - n; return true; } ++c; }
     } else if (bc == BC_OUTFLOW) {
-        if (ii == 0) for (int m = 0; m < g; ++m) { out[c] = m; flip[c] = 0; ++c; }
-        if (ii == n - 1) for (int m = 0; m < g; ++m) { out[c] = n + g + m; flip[c] = 0; ++c; }
+        if (ii == 0)
+            for (int m = 0; m < g; ++m) { if (idx == c) { o = m; return true; } ++c; }
+        if (ii == n - 1)
+            for (int m = 0; m < g; ++m) { if (idx == c) { o = n + g + m; return true; } ++c; }
     } else {
-        if (ii < g) { out[c] = g - 1 - ii; flip[c] = 1; ++c; }
-        if (ii >= n - g) { out[c] = 2 * n + g - 1 - ii; flip[c] = 1; ++c; }
+        if (ii < g) { if (idx == c) { o = g - 1 - ii; f = 1; return true; } ++c; }
+        if (ii >= n - g) { if (idx == c) { o = 2 * n + g - 1 - ii; f = 1; return true; } ++c; }
     }
-    return c;
+    return false;
 }
 
 // primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
@@ -264,21 +272,33 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
 #pragma unroll
         for (int q = 0; q < NQ; ++q) Pn[q] = LAW == LAW_RMHD ? Pold[q] : Pf[q * G.sP + pc];
     }
-    int ix[4], iy[4], iz[4], sx[4], sy[4], sz[4];
-    const int cx = guard_images_m(ii, G.n[0], G.g[0], G.bc, ix, sx);
-    const int cy = guard_images_m(jj, G.n[1], G.g[1], G.bc, iy, sy);
-    const int cz = guard_images_m(kk, G.n[2], G.g[2], G.bc, iz, sz);
-    for (int c = 0; c < cz; ++c)
-        for (int bb = 0; bb < cy; ++bb)
-            for (int a = 0; a < cx; ++a) {
-                const long long o = ((long long) iz[c] * G.N[1] + iy[bb]) * G.N[0] + ix[a];
+    // the zone's cell, then (zones within a guard width of an edge) its guard
+    // images on every combination of axes
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) Pf[q * G.sP + pc] = Pn[q];
+    const bool edge = (G.g[0] && (ii < G.g[0] || ii >= G.n[0] - G.g[0])) ||
+                      (G.g[1] && (jj < G.g[1] || jj >= G.n[1] - G.g[1])) ||
+                      (G.g[2] && (kk < G.g[2] || kk >= G.n[2] - G.g[2]));
+    if (!edge) return;
+    for (int c = 0; c <= G.g[2]; ++c) {
+        int oz, sz;
+        if (!guard_image_m(c, kk, G.n[2], G.g[2], G.bc, oz, sz)) continue;
+        for (int bb = 0; bb <= G.g[1]; ++bb) {
+            int oy, sy;
+            if (!guard_image_m(bb, jj, G.n[1], G.g[1], G.bc, oy, sy)) continue;
+            for (int a = 0; a <= G.g[0]; ++a) {
+                int ox, sx;
+                if ((a | bb | c) == 0 || !guard_image_m(a, ii, G.n[0], G.g[0], G.bc, ox, sx)) continue;
+                const long long o = ((long long) oz * G.N[1] + oy) * G.N[0] + ox;
 #pragma unroll
                 for (int q = 0; q < NQ; ++q) {
                     float v = Pn[q];
-                    if ((q == 1 && sx[a]) || (q == 2 && sy[bb]) || (q == 3 && sz[c])) v = -v;
+                    if ((q == 1 && sx) || (q == 2 && sy) || (q == 3 && sz)) v = -v;
                     Pf[q * G.sP + o] = v;
                 }
             }
+        }
+    }
 }
 
 template <int LAW>
