@@ -134,32 +134,6 @@ __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G,
     return V.at(a, q, i, j, k);
 }
 
-// image number idx of interior coordinate ii on one axis, or false where
-// there is none: 0 is the zone's own cell, then the guard cells that hold its
-// image (periodic: the copy across the grid; outflow: the whole guard layer
-// beside an edge zone; reflecting: the mirror cell, whose normal momentum
-// flips), as BoundaryCondition::applySimple fills them
-__device__ __forceinline__ bool guard_image_m(int idx, int ii, int n, int g, int bc, int& o, int& f)
-{
-    f = 0;
-    if (idx == 0) { o = ii + g; return true; }
-    if (g == 0) return false;
-    int c = 1;
-    if (bc == BC_PERIODIC) {
-        if (ii < g) { if (idx == c) { o = ii + g + n; return true; } ++c; }
-        if (ii >= n - g) { if (idx == c) { o = ii + g - n; return true; } ++c; }
-    } else if (bc == BC_OUTFLOW) {
-        if (ii == 0)
-            for (int m = 0; m < g; ++m) { if (idx == c) { o = m; return true; } ++c; }
-        if (ii == n - 1)
-            for (int m = 0; m < g; ++m) { if (idx == c) { o = n + g + m; return true; } ++c; }
-    } else {
-        if (ii < g) { if (idx == c) { o = g - 1 - ii; f = 1; return true; } ++c; }
-        if (ii >= n - g) { if (idx == c) { o = 2 * n + g - 1 - ii; f = 1; return true; } ++c; }
-    }
-    return false;
-}
-
 // primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
 // ConsToPrimRMHD for RMHD (the Newton iteration keeps FP64)
 template <int LAW>
@@ -282,13 +256,13 @@ __global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, f
     if (!edge) return;
     for (int c = 0; c <= G.g[2]; ++c) {
         int oz, sz;
-        if (!guard_image_m(c, kk, G.n[2], G.g[2], G.bc, oz, sz)) continue;
+        if (!guard_image(c, kk, G.n[2], G.g[2], G.bc, oz, sz)) continue;
         for (int bb = 0; bb <= G.g[1]; ++bb) {
             int oy, sy;
-            if (!guard_image_m(bb, jj, G.n[1], G.g[1], G.bc, oy, sy)) continue;
+            if (!guard_image(bb, jj, G.n[1], G.g[1], G.bc, oy, sy)) continue;
             for (int a = 0; a <= G.g[0]; ++a) {
                 int ox, sx;
-                if ((a | bb | c) == 0 || !guard_image_m(a, ii, G.n[0], G.g[0], G.bc, ox, sx)) continue;
+                if ((a | bb | c) == 0 || !guard_image(a, ii, G.n[0], G.g[0], G.bc, ox, sx)) continue;
                 const long long o = ((long long) oz * G.N[1] + oy) * G.N[0] + ox;
 #pragma unroll
                 for (int q = 0; q < NQ; ++q) {

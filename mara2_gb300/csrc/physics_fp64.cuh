@@ -828,4 +828,30 @@ __device__ __forceinline__ double max_eigen_magnitude(const double* A)
     return m;
 }
 
+// image number idx of interior coordinate ii on one axis, or false where
+// there is none: 0 is the zone's own cell, then the guard cells that hold its
+// image (periodic: the copy across the grid; outflow: the whole guard layer
+// beside an edge zone; reflecting: the mirror cell, whose normal momentum
+// flips), as BoundaryCondition::applySimple fills them
+__device__ __forceinline__ bool guard_image(int idx, int ii, int n, int g, int bc, int& o, int& f)
+{
+    f = 0;
+    if (idx == 0) { o = ii + g; return true; }
+    if (g == 0) return false;
+    int c = 1;
+    if (bc == BC_PERIODIC) {
+        if (ii < g) { if (idx == c) { o = ii + g + n; return true; } ++c; }
+        if (ii >= n - g) { if (idx == c) { o = ii + g - n; return true; } ++c; }
+    } else if (bc == BC_OUTFLOW) {
+        if (ii == 0)
+            for (int m = 0; m < g; ++m) { if (idx == c) { o = m; return true; } ++c; }
+        if (ii == n - 1)
+            for (int m = 0; m < g; ++m) { if (idx == c) { o = n + g + m; return true; } ++c; }
+    } else {
+        if (ii < g) { if (idx == c) { o = g - 1 - ii; f = 1; return true; } ++c; }
+        if (ii >= n - g) { if (idx == c) { o = 2 * n + g - 1 - ii; f = 1; return true; } ++c; }
+    }
+    return false;
+}
+
 } // namespace mara

@@ -143,24 +143,6 @@ __device__ __forceinline__ double face_flux(const FluxView& V, const GridDesc& G
 // Guard images of interior index ii along one axis: full indices that the
 // boundary condition fills with zone ii (first entry: the zone itself).
 // Returns the count; flip[m] marks reflected images.
-__device__ __forceinline__ int guard_images(int ii, int n, int g, int bc, int* out, int* flip)
-{
-    int c = 0;
-    out[c] = ii + g; flip[c] = 0; ++c;
-    if (g == 0) return c;
-    if (bc == BC_PERIODIC) {
-        if (ii < g) { out[c] = ii + g + n; flip[c] = 0; ++c; }
-        if (ii >= n - g) { out[c] = ii + g - n; flip[c] = 0; ++c; }
-    } else if (bc == BC_OUTFLOW) {
-        if (ii == 0) for (int m = 0; m < g; ++m) { out[c] = m; flip[c] = 0; ++c; }
-        if (ii == n - 1) for (int m = 0; m < g; ++m) { out[c] = n + g + m; flip[c] = 0; ++c; }
-    } else {
-        if (ii < g) { out[c] = g - 1 - ii; flip[c] = 1; ++c; }
-        if (ii >= n - g) { out[c] = 2 * n + g - 1 - ii; flip[c] = 1; ++c; }
-    }
-    return c;
-}
-
 template <int LAW>
 __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ Pin, double* __restrict__ Pout,
                                                      double* __restrict__ U0, double* __restrict__ U,
@@ -232,21 +214,27 @@ __global__ void __launch_bounds__(128) update_kernel(const double* __restrict__ 
         return;
     }
 
-    int ix[4], iy[4], iz[4], sx[4], sy[4], sz[4];
-    const int cx = guard_images(ii, G.n[0], G.g[0], G.bc, ix, sx);
-    const int cy = guard_images(jj, G.n[1], G.g[1], G.bc, iy, sy);
-    const int cz = guard_images(kk, G.n[2], G.g[2], G.bc, iz, sz);
-    for (int c = 0; c < cz; ++c)
-        for (int bb = 0; bb < cy; ++bb)
-            for (int a = 0; a < cx; ++a) {
-                const long long o = ((long long) iz[c] * G.N[1] + iy[bb]) * G.N[0] + ix[a];
+    // the zone's cell, then (zones within a guard width of an edge) its guard
+    // images on every combination of axes
+    for (int c = 0; c <= G.g[2]; ++c) {
+        int oz, sz;
+        if (!guard_image(c, kk, G.n[2], G.g[2], G.bc, oz, sz)) continue;
+        for (int bb = 0; bb <= G.g[1]; ++bb) {
+            int oy, sy;
+            if (!guard_image(bb, jj, G.n[1], G.g[1], G.bc, oy, sy)) continue;
+            for (int a = 0; a <= G.g[0]; ++a) {
+                int ox, sx;
+                if (!guard_image(a, ii, G.n[0], G.g[0], G.bc, ox, sx)) continue;
+                const long long o = ((long long) oz * G.N[1] + oy) * G.N[0] + ox;
 #pragma unroll
                 for (int q = 0; q < NQ; ++q) {
                     double v = Pn[q];
-                    if ((q == 1 && sx[a]) || (q == 2 && sy[bb]) || (q == 3 && sz[c])) v *= -1;
+                    if ((q == 1 && sx) || (q == 2 && sy) || (q == 3 && sz)) v *= -1;
                     Pout[q * G.sP + o] = v;
                 }
             }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
