@@ -134,6 +134,55 @@ __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G,
     return V.at(a, q, i, j, k);
 }
 
+// The 2-D (Z, W) Newton iteration of ConsToPrimRMHD (rm_anton2dzw, after
+// ConsToPrimRMHD::solve_anton2dzw, ConsToPrimRMHD.cpp:183-255) in reciprocal
+// form for the mixed path: 1/Z and
+// 1/W are formed once per iterate (and carried into the next iteration,
+// where the convergence test needs them too) and the Jacobian's inverse
+// from 1/det, so an iteration divides three times instead of about twenty;
+// FP64 division is a long instruction sequence on this GPU.  The update, the
+// clamps, the convergence test and the iteration cap are the reference's;
+// the iterates differ from the plain path's by rounding only.
+__device__ __forceinline__ int rm_anton2dzw_rcp(const C2pRmhd& s, double* P)
+{
+    const int bad = rm_check_cons(s.Cons);
+    if (bad) return bad;
+    int it = 0;
+    double error = 1.0, W = s.W_start, Z = s.Z_start;
+    const double D = s.D, Tau = s.Tau, S2 = s.S2, B2 = s.B2, BS2 = s.BS2, gamf = s.gamf;
+    const double iD = 1.0 / D;
+    double iW = 1.0 / W, iZ = 1.0 / Z;
+    while (error > 1e-12) {
+        const double Z2 = Z * Z, Z3 = Z * Z2, W2 = W * W;
+        const double iW2 = iW * iW, iW3 = iW2 * iW, iZ2 = iZ * iZ, iZ3 = iZ2 * iZ;
+        const double BZ = B2 + Z;
+        const double Pre = (D * iW) * (Z * iD * iW - 1.0) * gamf;
+        const double df0dZ = 2 * BZ * (BS2 * W2 + (W2 - 1) * Z3) * iW2 * iZ3;
+        const double df0dW = 2 * BZ * BZ * iW3;
+        const double df1dZ = 1.0 + BS2 * iZ3 - gamf * iW2;
+        const double df1dW = B2 * iW3 + (2 * Z - D * W) * iW3 * gamf;
+        const double f0 = -S2 + BZ * BZ * (W2 - 1) * iW2 - (2 * Z + B2) * BS2 * iZ2;
+        const double f1 = -Tau + Z + B2 - Pre - 0.5 * B2 * iW2 - 0.5 * BS2 * iZ2 - D;
+        const double idet = 1.0 / (df0dZ * df1dW - df0dW * df1dZ);
+        const double dZ = -(df1dW * f0 - df0dW * f1) * idet;
+        const double dW = -(df0dZ * f1 - df1dZ * f0) * idet;
+        double Z_new = Z + dZ;
+        double W_new = W + dW;
+        Z_new = (Z_new > 0.0) ? Z_new : -Z_new;
+        Z_new = (Z_new < 1e20) ? Z_new : Z;
+        W_new = (W_new > 1.0) ? W_new : 1.0;
+        W_new = (W_new < 1e12) ? W_new : 1e12;
+        Z = Z_new;
+        W = W_new;
+        iZ = 1.0 / Z;
+        iW = 1.0 / W;
+        error = fabs(dZ * iZ) + fabs(dW * iW);
+        ++it;
+        if (it == 250) return ST_C2P_MAXITER;
+    }
+    return rm_reconstruct(s, Z, W, P);
+}
+
 // primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
 // ConsToPrimRMHD for RMHD (the Newton iteration keeps FP64)
 template <int LAW>
@@ -191,7 +240,7 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
                 s.W_start = sqrt(W2);
             }
         }
-        int err = rm_anton2dzw(s, Pd);
+        int err = rm_anton2dzw_rcp(s, Pd);
         if (err != ST_OK) err = rm_noble1dw(s, Pd);
         if (err != ST_OK) { *code = err; return ST_INVERSION_FAILURE; }
 #pragma unroll
