@@ -28,11 +28,11 @@ constexpr int CLUSTER1D_MAX_CTAS = 8;  // portable cluster size
 constexpr int CLUSTER1D_MAX_ZONES_PER_CTA = 1024;
 
 // dynamic shared memory of a CTA holding m zones with a halo of G: U hi/lo
-// and U0 hi/lo (5 fields each), primitives with halo, face fluxes, the
-// CTA's Courant slot
+// and U0 hi/lo (5 fields each), two buffers of primitives with halo (stages
+// alternate), face fluxes, two Courant slots (steps alternate)
 __host__ __device__ constexpr size_t cluster1d_smem_bytes(int m, int G)
 {
-    return sizeof(float) * (4 * 5 * (size_t) m + 5 * (size_t) (m + 2 * G) + 5 * (size_t) (m + 1) + 4);
+    return sizeof(float) * (4 * 5 * (size_t) m + 2 * 5 * (size_t) (m + 2 * G) + 5 * (size_t) (m + 1) + 4);
 }
 
 // What one launch advances: cluster c of the launch runs the driver loop of
@@ -85,10 +85,10 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
     float* Ul = Uh + 5 * m;
     float* U0h = Ul + 5 * m;
     float* U0l = U0h + 5 * m;
-    float* Ps = U0l + 5 * m;                       // [5][m + 2G], zone z at z + G
-    float* Fx = Ps + 5 * (m + 2 * G);              // [5][m + 1]
-    float* red = Fx + 5 * (m + 1);                 // this CTA's Courant slot
     const int W = m + 2 * G;
+    float* Pbuf = U0l + 5 * m;                     // 2 x [5][W], zone z at z + G
+    float* Fx = Pbuf + 2 * 5 * W;                  // [5][m + 1]
+    float* red = Fx + 5 * (m + 1);                 // this CTA's Courant slots, [2]
     __shared__ float wmin[32];
     float* __restrict__ gh = s == 0 ? g.Uh[0] : s == 1 ? g.Uh[1] : g.Uh[2];
     float* __restrict__ gl = s == 0 ? g.Ul[0] : s == 1 ? g.Ul[1] : g.Ul[2];
@@ -107,24 +107,23 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
     double dt = job.dt[slot];
     unsigned long long bits = job.cfl[slot];
     unsigned long long used = job.used ? job.used[slot] : 0ull;
-    cluster.sync();
 
-    for (int step = 0; step < job.nsteps && !done; ++step) {
-        // the step start of the fused path (k_fused_run_begin)
-        used = bits;
-        dt = cfl * __longlong_as_double((long long) bits);
-        if (t_final >= 0.0) {
-            if (!(t < t_final)) { done = 1; break; }
-            const double dt2 = t_final - t;
-            dt = dt < dt2 ? dt : dt2;
-        }
-        const float dtf = (float) dt;
+    // One cluster barrier per RK stage, after the primitives are formed: the
+    // primitives alternate between two buffers by stage, so a neighbour's
+    // halo reads of one stage end (it reaches the next barrier) before this
+    // CTA writes that buffer again two stages later; the Courant slots
+    // alternate by step, read by every CTA after the first barrier of the
+    // next step and written again after the second.
+    int par = 0;                                   // the stage's buffer
+    int step = 0;
+    for (; step < job.nsteps && !done; ++step) {
         float zdt = 3.0e38f;
-        for (int rk = 0; rk < order; ++rk) {
+        for (int rk = 0; rk < order; ++rk, par ^= 1) {
             const int last = rk == order - 1;
             const float b = order == 1 ? 1.f : order == 2 ? (rk == 0 ? 1.f : 0.5f)
                                                           : (rk == 0 ? 1.f : rk == 1 ? 0.25f : 2.f / 3.f);
             const float omb = 1.f - b;
+            float* Ps = Pbuf + par * 5 * W;
             // 1. primitives of the owned zones (from the high words)
             for (int i = threadIdx.x; i < mine; i += blockDim.x) {
                 float U[5], P[5];
@@ -135,6 +134,25 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                 for (int q = 0; q < 5; ++q) Ps[q * W + G + i] = P[q];
             }
             cluster.sync();
+            if (rk == 0) {
+                // the step start of the fused path (k_fused_run_begin): the
+                // Courant step of the state, from the previous step's slots
+                // (the first step of a launch takes the one it was given)
+                if (step > 0) {
+                    float mn = 3.0e38f;
+                    for (int k = 0; k < C; ++k) mn = fminf(mn, cluster.map_shared_rank(red, k)[(step - 1) & 1]);
+                    // no valid zone leaves the slot at its reset value, as in the fused path
+                    bits = (unsigned long long) __double_as_longlong(mn < 3.0e38f ? (double) mn : DBL_MAX);
+                }
+                used = bits;
+                dt = cfl * __longlong_as_double((long long) bits);
+                if (t_final >= 0.0) {
+                    if (!(t < t_final)) { done = 1; break; }
+                    const double dt2 = t_final - t;
+                    dt = dt < dt2 ? dt : dt2;
+                }
+            }
+            const float dtf = (float) dt;
             // 2. the halo: 2G zones from the neighbours' shared memory, or the
             //    boundary image of the grid's edge (momentum negated across a
             //    reflecting boundary)
@@ -200,25 +218,23 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                 if (threadIdx.x == 0) {
                     float w = 3.0e38f;
                     for (int k = 0; k < (int) (blockDim.x + 31) / 32; ++k) w = fminf(w, wmin[k]);
-                    red[0] = w;
+                    red[step & 1] = w;
                 }
             }
-            // neighbours have read this CTA's primitives before they change,
-            // and every CTA's Courant part is in place
-            cluster.sync();
         }
-        // the slots are next written in the last stage of the next step,
-        // after at least one more cluster barrier, which no CTA reaches
-        // before it has read them here
-        float mn = 3.0e38f;
-        for (int k = 0; k < C; ++k) mn = fminf(mn, cluster.map_shared_rank(red, k)[0]);
-        // no valid zone leaves the slot at its reset value, as in the fused path
-        bits = (unsigned long long) __double_as_longlong(mn < 3.0e38f ? (double) mn : DBL_MAX);
+        if (done) break;
         t += dt;
         steps += 1;
         // the next step's start would stop here: stop now, so that a grid
         // finishing on a launch's last step is reported by that launch
-        if (t_final >= 0.0 && !(t < t_final)) done = 1;
+        if (t_final >= 0.0 && !(t < t_final)) { done = 1; ++step; break; }
+    }
+    // the Courant step of the last step taken, once every CTA's slot is in
+    cluster.sync();
+    if (step > 0) {
+        float mn = 3.0e38f;
+        for (int k = 0; k < C; ++k) mn = fminf(mn, cluster.map_shared_rank(red, k)[(step - 1) & 1]);
+        bits = (unsigned long long) __double_as_longlong(mn < 3.0e38f ? (double) mn : DBL_MAX);
     }
     for (int i = threadIdx.x; i < mine; i += blockDim.x) {
 #pragma unroll
@@ -227,7 +243,8 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
             gl[q * g.sU + z0 + i] = Ul[q * m + i];
         }
     }
-    // the clock is published after every CTA's part of the state
+    // the clock is published after every CTA's part of the state; the slots
+    // are read before any CTA leaves
     __threadfence();
     cluster.sync();
     if (r == 0 && threadIdx.x == 0) {
