@@ -25,6 +25,7 @@
 namespace mara {
 
 constexpr int CLUSTER1D_MAX_CTAS = 8;  // portable cluster size
+constexpr int CLUSTER1D_WIDE_CTAS = 16; // the non-portable size, where the GPU can place it
 constexpr int CLUSTER1D_MAX_ZONES_PER_CTA = 1024;
 
 // dynamic shared memory of a CTA holding m zones with a halo of G: U hi/lo
@@ -259,35 +260,66 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
 }
 
 // grid of cluster_count clusters of C CTAs, each CTA sized for up to m zones
+// the launch configuration of cluster_count clusters of C CTAs sized for up
+// to m zones each (at[] must outlive the returned configuration)
 template <int RECON, int RIEMANN>
-inline cudaError_t launch_cluster1d(const Cluster1DJob& job, int cluster_count, int C, int m, cudaStream_t stream)
+inline cudaError_t cluster1d_config(int cluster_count, int C, int m, cudaStream_t stream, cudaLaunchAttribute* at,
+                                    cudaLaunchConfig_t& lc)
 {
     constexpr int G = HaloOf<RECON>::G;
     const size_t smem = cluster1d_smem_bytes(m, G);
     const int threads = m + 1 < 1024 ? ((m + 1 + 31) / 32) * 32 : 1024;  // one thread per face
     auto k = hydro_cluster1d_kernel<RECON, RIEMANN>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e == cudaSuccess && C > CLUSTER1D_MAX_CTAS)
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = (unsigned) C;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cudaLaunchConfig_t lc = {};
+    lc = {};
     lc.gridDim = dim3((unsigned) (cluster_count * C));
     lc.blockDim = dim3((unsigned) threads);
     lc.dynamicSmemBytes = smem;
     lc.stream = stream;
     lc.attrs = at;
     lc.numAttrs = 1;
-    return cudaLaunchKernelEx(&lc, k, job);
+    return cudaSuccess;
 }
 
-// CTAs of a grid of n zones: every CTA owns at least 128 zones
-inline int cluster1d_ctas(int n)
+// grid of cluster_count clusters of C CTAs, each CTA sized for up to m zones
+template <int RECON, int RIEMANN>
+inline cudaError_t launch_cluster1d(const Cluster1DJob& job, int cluster_count, int C, int m, cudaStream_t stream)
+{
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t lc;
+    const cudaError_t e = cluster1d_config<RECON, RIEMANN>(cluster_count, C, m, stream, at, lc);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&lc, hydro_cluster1d_kernel<RECON, RIEMANN>, job);
+}
+
+// can the GPU place one cluster of C CTAs sized for m zones?
+template <int RECON, int RIEMANN>
+inline bool cluster1d_fits(int C, int m)
+{
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t lc;
+    int n = 0;
+    if (cluster1d_config<RECON, RIEMANN>(1, C, m, nullptr, at, lc) != cudaSuccess ||
+        cudaOccupancyMaxActiveClusters(&n, hydro_cluster1d_kernel<RECON, RIEMANN>, &lc) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
+// CTAs of a grid of n zones: every CTA owns at least 128 zones, at most
+// `cap` CTAs
+inline int cluster1d_ctas(int n, int cap = CLUSTER1D_MAX_CTAS)
 {
     const int c = n / 128;
-    return c < 1 ? 1 : c > CLUSTER1D_MAX_CTAS ? CLUSTER1D_MAX_CTAS : c;
+    return c < 1 ? 1 : c > cap ? cap : c;
 }
 
 } // namespace mara

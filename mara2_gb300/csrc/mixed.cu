@@ -1356,7 +1356,11 @@ template <int RECON, int RIEMANN>
 static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
 {
     const int n = m->G.n[0];
-    const int C = cluster1d_ctas(n);
+    // a single grid is latency-bound: up to the wide cluster size where it
+    // fits (a step of 8192 zones: 11.9 us on 8 CTAs, 8.5 us on 16)
+    int C = cluster1d_ctas(n);
+    const int wide = cluster1d_ctas(n, CLUSTER1D_WIDE_CTAS);
+    if (wide > C && cluster1d_fits<RECON, RIEMANN>(wide, (n + wide - 1) / wide)) C = wide;
     Cluster1DJob job = {};
     job.grids = m->dgrid;
     job.t = &st->t;
