@@ -84,15 +84,44 @@ __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P
 
 struct FluxViewF {
     const float* F[3];
+    const float* E[3];   // edge EMFs of the flux CT (pairs x-y, x-z, y-z), or null
     long long sF;
     int M0, M1;
     __device__ __forceinline__ float at(int a, int q, int i, int j, int k) const
     {
         return F[a][q * sF + ((long long) k * M1 + j) * M0 + i];
     }
+    __device__ __forceinline__ float emf(int e, int i, int j, int k) const
+    {
+        return E[e][((long long) k * M1 + j) * M0 + i];
+    }
 };
 
-// flux CT of CellCenteredFieldCT::correctGodunovFluxes on one face (FP32)
+// The edge EMFs of CellCenteredFieldCT::correctGodunovFluxes (Toth 2000,
+// eq. 25), each formed once from the four face fluxes around its edge: for
+// axes a < b, E_ab at the edge below face index (i, j, k) on both axes is
+// (F_a[B_b] + F_a[B_b](-1 along b) - F_b[B_a] - F_b[B_a](-1 along a)) / 4.
+// A corrected flux is then the mean of the two EMFs on its face's edges
+// (face_flux_f), which is the reference's 1/8-weighted stencil.
+__global__ void __launch_bounds__(128) ct_emf_kernel(FluxViewF V, float* E01, float* E02, float* E12, int M0, int M1,
+                                                     int M2, int fx, int fy, int fz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= M0) return;
+    const long long e = ((long long) k * M1 + j) * M0 + i;
+    constexpr int B0 = 5, B1 = 6, B2 = 7;
+    if (fx && fy && i > 0 && j > 0)
+        E01[e] = 0.25f * (V.at(0, B1, i, j, k) + V.at(0, B1, i, j - 1, k) - V.at(1, B0, i, j, k) - V.at(1, B0, i - 1, j, k));
+    if (fx && fz && i > 0 && k > 0)
+        E02[e] = 0.25f * (V.at(0, B2, i, j, k) + V.at(0, B2, i, j, k - 1) - V.at(2, B0, i, j, k) - V.at(2, B0, i - 1, j, k));
+    if (fy && fz && j > 0 && k > 0)
+        E12[e] = 0.25f * (V.at(1, B2, i, j, k) + V.at(1, B2, i, j, k - 1) - V.at(2, B1, i, j, k) - V.at(2, B1, i, j - 1, k));
+    (void) M2;
+}
+
+// flux CT of CellCenteredFieldCT::correctGodunovFluxes on one face (FP32):
+// the normal field's flux is zero, a tangential field's the mean of the edge
+// EMFs (ct_emf_kernel) on the face's two edges along the other axis
 template <int NQ>
 __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G, int a, int q, int i, int j, int k)
 {
@@ -101,34 +130,16 @@ __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G,
         const int B0 = 5, B1 = 6, B2 = 7;
         if (a == 0) {
             if (q == B0) return 0.f;
-            if (q == B1 && fy)
-                return 0.125f * (2.f * V.at(0, B1, i, j, k) + V.at(0, B1, i, j + 1, k) + V.at(0, B1, i, j - 1, k)
-                                 - V.at(1, B0, i, j + 1, k) - V.at(1, B0, i - 1, j + 1, k)
-                                 - V.at(1, B0, i, j, k) - V.at(1, B0, i - 1, j, k));
-            if (q == B2 && fz)
-                return 0.125f * (2.f * V.at(0, B2, i, j, k) + V.at(0, B2, i, j, k + 1) + V.at(0, B2, i, j, k - 1)
-                                 - V.at(2, B0, i, j, k + 1) - V.at(2, B0, i - 1, j, k + 1)
-                                 - V.at(2, B0, i, j, k) - V.at(2, B0, i - 1, j, k));
+            if (q == B1 && fy) return 0.5f * (V.emf(0, i, j + 1, k) + V.emf(0, i, j, k));
+            if (q == B2 && fz) return 0.5f * (V.emf(1, i, j, k + 1) + V.emf(1, i, j, k));
         } else if (a == 1) {
             if (q == B1) return 0.f;
-            if (q == B2 && fz)
-                return 0.125f * (2.f * V.at(1, B2, i, j, k) + V.at(1, B2, i, j, k + 1) + V.at(1, B2, i, j, k - 1)
-                                 - V.at(2, B1, i, j, k + 1) - V.at(2, B1, i, j - 1, k + 1)
-                                 - V.at(2, B1, i, j, k) - V.at(2, B1, i, j - 1, k));
-            if (q == B0 && fx)
-                return 0.125f * (2.f * V.at(1, B0, i, j, k) + V.at(1, B0, i + 1, j, k) + V.at(1, B0, i - 1, j, k)
-                                 - V.at(0, B1, i + 1, j, k) - V.at(0, B1, i + 1, j - 1, k)
-                                 - V.at(0, B1, i, j, k) - V.at(0, B1, i, j - 1, k));
+            if (q == B2 && fz) return 0.5f * (V.emf(2, i, j, k + 1) + V.emf(2, i, j, k));
+            if (q == B0 && fx) return -0.5f * (V.emf(0, i + 1, j, k) + V.emf(0, i, j, k));
         } else {
             if (q == B2) return 0.f;
-            if (q == B0 && fx)
-                return 0.125f * (2.f * V.at(2, B0, i, j, k) + V.at(2, B0, i + 1, j, k) + V.at(2, B0, i - 1, j, k)
-                                 - V.at(0, B2, i + 1, j, k) - V.at(0, B2, i + 1, j, k - 1)
-                                 - V.at(0, B2, i, j, k) - V.at(0, B2, i, j, k - 1));
-            if (q == B1 && fy)
-                return 0.125f * (2.f * V.at(2, B1, i, j, k) + V.at(2, B1, i, j + 1, k) + V.at(2, B1, i, j - 1, k)
-                                 - V.at(1, B2, i, j + 1, k) - V.at(1, B2, i, j + 1, k - 1)
-                                 - V.at(1, B2, i, j, k) - V.at(1, B2, i, j, k - 1));
+            if (q == B0 && fx) return -0.5f * (V.emf(1, i + 1, j, k) + V.emf(1, i, j, k));
+            if (q == B1 && fy) return -0.5f * (V.emf(2, i, j + 1, k) + V.emf(2, i, j, k));
         }
     }
     return V.at(a, q, i, j, k);
@@ -504,6 +515,7 @@ struct MixedState {
     float** dUl = nullptr;
     float* Pf = nullptr;
     float* F[3] = {nullptr, nullptr, nullptr};
+    float* E[3] = {nullptr, nullptr, nullptr};  // flux-CT edge EMFs (magnetic laws)
     HGrid* dgrid = nullptr;
     TileRef* dtiles = nullptr;
     int ntiles = 0;
@@ -572,6 +584,8 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
         rc = dev_alloc((void**) &m->Pf, sizeof(float) * G.sP * nq, s, bytes);
         for (int a = 0; a < 3 && !rc; ++a)
             if (G.n[a] > 1) rc = dev_alloc((void**) &m->F[a], sizeof(float) * G.sF * nq, s, bytes);
+        if (G.ct && nq == 8)
+            for (int e = 0; e < 3 && !rc; ++e) rc = dev_alloc((void**) &m->E[e], sizeof(float) * G.sF, s, bytes);
     }
     if (!rc && m->fused) {
         HGrid h;
@@ -619,6 +633,7 @@ void mixed_destroy(MixedState* m)
     cudaFree(m->dUh); cudaFree(m->dUl); cudaFree(m->drot); cudaFree(m->dcfl);
     cudaFree(m->Pf);
     for (int a = 0; a < 3; ++a) cudaFree(m->F[a]);
+    for (int e = 0; e < 3; ++e) cudaFree(m->E[e]);
     cudaFree(m->dgrid);
     cudaFree(m->dtiles);
     cudaFree(m->dntiles);
@@ -786,6 +801,7 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
     const int* done = &st->done;
     FluxViewF V;
     for (int a = 0; a < 3; ++a) V.F[a] = m->F[a];
+    for (int e = 0; e < 3; ++e) V.E[e] = m->E[e];
     V.sF = m->G.sF;
     V.M0 = m->G.N[0] + 1;
     V.M1 = m->G.N[1] + 1;
@@ -799,6 +815,13 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
                     case MARA_LAW_MHD: flux_f<LAW_MHD>(m, a, done, st, s); break;
                     default: flux_f<LAW_RMHD>(m, a, done, st, s); break;
                 }
+            });
+        }
+        if (m->E[0]) {
+            dim3 eg((V.M0 + 127) / 128, V.M1, m->G.N[2] + 1);
+            timed(m, s, [&] {
+                ct_emf_kernel<<<eg, 128, 0, s>>>(V, m->E[0], m->E[1], m->E[2], V.M0, V.M1, m->G.N[2] + 1,
+                                                 m->G.n[0] > 1, m->G.n[1] > 1, m->G.n[2] > 1);
             });
         }
         const float b = B_TAB[order - 1][rk];
