@@ -154,6 +154,30 @@ __device__ __forceinline__ float face_flux_f(const FluxViewF& V, const GridF& G,
 // FP64 division is a long instruction sequence on this GPU.  The update, the
 // clamps, the convergence test and the iteration cap are the reference's;
 // the iterates differ from the plain path's by rounding only.
+// ConsToPrimRMHD::reconstruct_prim (ConsToPrimRMHD.cpp:110-145) from the
+// root (Z, W) and their reciprocals, with reciprocals instead of divisions
+__device__ __forceinline__ int rm_reconstruct_rcp(const C2pRmhd& s, double Z, double W, double iZ, double iW,
+                                                  double* Pout)
+{
+    double P[8];
+    const double iZB = 1.0 / (Z + s.B2);
+    const double b0 = s.BS * W * iZ;
+    P[0] = s.D * iW;
+    P[4] = P[0] * (Z * iW / s.D - 1.0) * s.gamf;
+    P[1] = (s.Cons[1] + b0 * s.Cons[5] * iW) * iZB;
+    P[2] = (s.Cons[2] + b0 * s.Cons[6] * iW) * iZB;
+    P[3] = (s.Cons[3] + b0 * s.Cons[7] * iW) * iZB;
+    P[5] = s.Cons[5];
+    P[6] = s.Cons[6];
+    P[7] = s.Cons[7];
+    if (P[4] <= 0.0 && s.pfloor > 0.0) P[4] = P[0] * s.pfloor;
+    const int err = rm_check_prim(P);
+    if (err) return err;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Pout[q] = P[q];
+    return ST_OK;
+}
+
 __device__ __forceinline__ int rm_anton2dzw_rcp(const C2pRmhd& s, double* P)
 {
     const int bad = rm_check_cons(s.Cons);
@@ -191,7 +215,7 @@ __device__ __forceinline__ int rm_anton2dzw_rcp(const C2pRmhd& s, double* P)
         ++it;
         if (it == 250) return ST_C2P_MAXITER;
     }
-    return rm_reconstruct(s, Z, W, P);
+    return rm_reconstruct_rcp(s, Z, W, iZ, iW, P);
 }
 
 // primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
@@ -236,8 +260,7 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
         s.BS2 = s.BS * s.BS;
 #pragma unroll
         for (int q = 0; q < 8; ++q) s.Cons[q] = U[q];
-        s.Z_start = sqrt(s.S2 + s.D * s.D);
-        s.W_start = s.Z_start / s.D;
+        bool warm = false;
         if (Pprev) {
             // warm start from the zone's primitives of the previous stage
             // (ConsToPrimRMHD::set_starting_prim, ConsToPrimRMHD.cpp:99-108):
@@ -246,10 +269,16 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
             const double V2 = (double) Pprev[1] * Pprev[1] + (double) Pprev[2] * Pprev[2] + (double) Pprev[3] * Pprev[3];
             if (rho > 0.0 && pre > 0.0 && V2 < 1.0) {
                 const double W2 = 1.0 / (1.0 - V2);
-                const double h = 1.0 + pre / (rho * (pp.gamma - 1.0)) + pre / rho;
+                const double h = 1.0 + pre / rho * (G.inv_gm1_d + 1.0);
                 s.Z_start = rho * h * W2;
                 s.W_start = sqrt(W2);
+                warm = true;
             }
+        }
+        if (!warm) {
+            // the cold start of ConsToPrimRMHD::estimate_from_cons (ConsToPrimRMHD.cpp:88-92)
+            s.Z_start = sqrt(s.S2 + s.D * s.D);
+            s.W_start = s.Z_start / s.D;
         }
         int err = rm_anton2dzw_rcp(s, Pd);
         if (err != ST_OK) err = rm_noble1dw(s, Pd);
