@@ -20,6 +20,7 @@
 #ifndef MARA_GPU_H
 #define MARA_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -117,6 +118,12 @@ int mara_gpu_destroy(MaraGpuHandle* handle);
  * marks the end. */
 int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos);
 int mara_gpu_download(MaraGpuHandle* h, double* P_aos);
+
+/* Page-lock a host array (MeshData::P) of `bytes` bytes, or undo it, so that
+ * the host calls above and mara_gpu_advance_host read and write it in place
+ * (cudaHostRegister, mapped).  MARA_ERR_CUDA if the driver refuses. */
+int mara_gpu_host_register(void* p, size_t bytes);
+int mara_gpu_host_unregister(void* p);
 
 /* MethodOfLinesTVD::advance (SolutionSchemes.cpp:108-275) on the resident
  * state: every RK stage, flux CT when the law is magnetic, primitive recovery

@@ -84,6 +84,8 @@ SIGNATURES = {
     "mara_gpu_synchronize": (C.c_int, [_H]),
     "mara_gpu_stats": (C.c_int, [_H, C.POINTER(MaraGpuStats)]),
     "mara_gpu_stream": (C.c_void_p, [_H]),
+    "mara_gpu_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "mara_gpu_host_unregister": (C.c_int, [C.c_void_p]),
     "mara_gpu_set_kernel_timing": (C.c_int, [_H, C.c_int]),
     "mara_gpu_kernel_times": (C.c_int, [_H, _D, C.POINTER(C.c_int64)]),
     "mara_gpu_device_bytes": (C.c_int64, [_H]),

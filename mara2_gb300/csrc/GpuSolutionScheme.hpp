@@ -47,6 +47,10 @@ struct GpuSchemeOptions
     Coordinate upper = {{1.0, 1.0, 1.0}};
     int precision = MARA_PRECISION_FP64;
     int device = 0;
+    // page-lock MeshData::P on the first advance (and again if the array
+    // moves), so advance() reads and writes it in place; for a 2-D mixed
+    // hydro grid the transfers then overlap the stages (mara_gpu_advance_host)
+    bool pinHostState = false;
 };
 
 class GpuMethodOfLinesTVD : public SolutionScheme
@@ -56,7 +60,11 @@ public:
 
     GpuMethodOfLinesTVD() {}
     explicit GpuMethodOfLinesTVD (Options options) : opts (options) {}
-    ~GpuMethodOfLinesTVD() { if (handle) mara_gpu_destroy (handle); }
+    ~GpuMethodOfLinesTVD()
+    {
+        if (handle) mara_gpu_destroy (handle);
+        if (pinned) mara_gpu_host_unregister (pinned);
+    }
     GpuMethodOfLinesTVD (const GpuMethodOfLinesTVD&) = delete;
     GpuMethodOfLinesTVD& operator= (const GpuMethodOfLinesTVD&) = delete;
 
@@ -82,6 +90,13 @@ public:
     void advance (MeshData& solution, double t0, double dt) const override
     {
         ensure (solution);
+        if (opts.pinHostState && pinned != solution.P.data())
+        {
+            if (pinned) mara_gpu_host_unregister (pinned);
+            pinned = nullptr;
+            if (mara_gpu_host_register (solution.P.data(), solution.P.size() * sizeof (double)) == MARA_OK)
+                pinned = solution.P.data();
+        }
         raise (mara_gpu_advance_host (handle, solution.P.data(), t0, dt));
     }
 
@@ -210,4 +225,5 @@ private:
     std::shared_ptr<MeshOperator> meshOperator;
     std::shared_ptr<IntercellFluxScheme> fluxScheme;
     mutable MaraGpuHandle* handle = nullptr;
+    mutable double* pinned = nullptr;   // the page-locked MeshData::P, if any
 };

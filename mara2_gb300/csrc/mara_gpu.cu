@@ -551,6 +551,26 @@ static const void* direct_host_pointer(const void* p)
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+int mara_gpu_host_register(void* p, size_t bytes)
+{
+    if (!p || !bytes) return MARA_ERR_ARGUMENT;
+    if (cudaHostRegister(p, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped) != cudaSuccess) {
+        cudaGetLastError();
+        return MARA_ERR_CUDA;
+    }
+    return MARA_OK;
+}
+
+int mara_gpu_host_unregister(void* p)
+{
+    if (!p) return MARA_ERR_ARGUMENT;
+    if (cudaHostUnregister(p) != cudaSuccess) {
+        cudaGetLastError();
+        return MARA_ERR_CUDA;
+    }
+    return MARA_OK;
+}
+
 int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;

@@ -249,3 +249,25 @@ def test_pipelined_host_step_rectangular(gpu_lib, ni, nj, bc):
             a.advance_host(ref, dt)
             assert b.advance_host_ptr(pin.data_ptr(), dt) == 0
         assert np.array_equal(pin.numpy().view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_host_register_makes_an_array_page_locked(gpu_lib):
+    """mara_gpu_host_register page-locks a caller's array (the C++ drop-in's
+    pinHostState): advance_host then reads and writes it in place, with the
+    bits of the pageable path."""
+    from mara2_gb300 import _native as N
+    s, P = W.kelvin_helmholtz(256)
+    lib = N.load()
+    with Solver(s, "mixed") as a, Solver(s, "mixed") as b:
+        a.upload(P.copy())
+        dt = a.courant() * s.cfl
+        ref = P.copy()
+        a.advance_host(ref, dt)
+        arr = np.ascontiguousarray(P.copy())
+        assert lib.mara_gpu_host_register(arr.ctypes.data, arr.nbytes) == 0
+        try:
+            assert b.advance_host_ptr(arr.ctypes.data, dt) == 0
+        finally:
+            assert lib.mara_gpu_host_unregister(arr.ctypes.data) == 0
+        assert np.array_equal(arr.view(np.uint64), ref.view(np.uint64))
