@@ -83,6 +83,31 @@ def test_cluster_slots_match_lockstep(gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("rk,recon,riemann", [(1, "pcm", "hlle"), (3, "plm", "hlle")])
+def test_cluster_slots_match_lockstep_other_schemes(gpu_lib, rk, recon, riemann):
+    """The same comparison for RK1 (the lockstep path swaps the state buffer
+    every step, the clusters update in place) and RK3, PCM and HLLE."""
+    reqs = W.riemann_stream(40, rate=1e6, seed=11, n1=(64, 512), n2=(32, 64))
+    one = [r for r in reqs if r.dims == 1][:3]
+    two = [r for r in reqs if r.dims == 2][:2]
+    built = []
+    for r, n in zip(one, [100, 700, 3000]):
+        s, P = W.riemann_initial(dataclasses.replace(r, n=n))
+        built.append((s.with_(t_final=0.004, rk_order=rk, recon=recon, riemann=riemann, guard=2), P))
+    for r in two:
+        s, P = _make(r)
+        built.append((s.with_(rk_order=rk, recon=recon, riemann=riemann, guard=2), P))
+    kw = dict(recon=recon, riemann=riemann, rk_order=rk)
+    a = _run_batch(built, **kw)
+    b = _run_batch(built, lockstep_1d=True, **kw)
+    for k, (s, _) in enumerate(built):
+        Pa, ta, na = a[k]
+        Pb, tb, nb = b[k]
+        assert na == nb and ta == tb, (k, na, nb, ta, tb)
+        assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), k
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [300, 5000])
 def test_cluster_slot_matches_single_grid_run(gpu_lib, n):
     """A 1-D grid in the batch and the same grid run by a single-grid handle
