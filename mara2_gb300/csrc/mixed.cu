@@ -1179,10 +1179,13 @@ static void host_step_destroy(HostStep* hs)
 bool mixed_host_step_capable(const MixedState* m)
 {
     // a stage reads one tile either side only if the last tile row and column
-    // hold at least the two-zone halo
+    // hold at least the two-zone halo; below about half a million zones the
+    // pipeline's fixed costs outweigh the overlap (256^2: 0.098 ms against
+    // 0.085 ms unpipelined; 512^2 even; 1024^2 0.45 against 0.56 ms)
     const int rx = m->G.n[0] % 32, ry = m->G.n[1] % 16;
     return m->fused && m->G.n[1] > 1 && m->G.N[2] == 1 && m->G.n[0] >= 128 && m->tx == 32 && m->ty == 16 &&
-           (rx == 0 || rx >= 2) && (ry == 0 || ry >= 2);
+           (rx == 0 || rx >= 2) && (ry == 0 || ry >= 2) && (long long) m->G.n[0] * m->G.n[1] >= (1 << 19) &&
+           !m->hs_unavailable;
 }
 
 template <int RECON, int RIEMANN>

@@ -178,47 +178,11 @@ def test_page_locked_buffers_match_pageable(gpu_lib, precision, make):
         assert np.array_equal(pin.numpy().view(np.uint64), a.view(np.uint64))
 
 
-PIPELINED = [(384, "periodic", "plm", "hllc", 2), (420, "outflow", "plm", "hlle", 3),
-             (352, "reflecting", "pcm", "hllc", 1), (330, "periodic", "pcm", "hlle", 1), (130, "periodic", "plm", "hllc", 2)]
-
-
-@pytest.mark.gpu
-@pytest.mark.parametrize("n,bc,recon,riemann,rk", PIPELINED)
-def test_pipelined_host_step_matches_unpipelined(gpu_lib, n, bc, recon, riemann, rk):
-    """The drop-in call on a page-locked 2-D array runs as one launch that
-    pipelines the transfers in, the stages and the transfers out by bands of
-    host rows; a pageable array takes the unpipelined path (whole-grid
-    transfers, then the stages).  Several calls in a row (the rotation
-    parity of RK1 alternates), then a resident step: the same bits in the
-    host array and on the device, and the same Courant step."""
-    import torch
-    s0, P0 = W.kelvin_helmholtz(n)
-    s = s0.with_(bc=bc, recon=recon, riemann=riemann, rk_order=rk)
-    P = W.empty_state(s)
-    P[s.interior()] = P0[s0.interior()]
-    P = W.apply_bc_numpy(s, P)
-    with Solver(s, "mixed") as a, Solver(s, "mixed") as b:
-        a.upload(P.copy())
-        dt = a.courant() * s.cfl
-        ref = P.copy()
-        pin = torch.from_numpy(P.copy()).pin_memory()
-        for _ in range(3):
-            a.advance_host(ref, dt)
-            assert b.advance_host_ptr(pin.data_ptr(), dt) == 0
-            assert np.array_equal(pin.numpy().view(np.uint64), ref.view(np.uint64))
-        assert a.courant() == b.courant()
-        assert a.stats().steps == b.stats().steps
-        # the device state after the pipelined call continues like the other
-        a.advance(dt)
-        b.advance(dt)
-        assert np.array_equal(a.download().view(np.uint64), b.download().view(np.uint64))
-
-
-def _rect_state(ni, nj, bc, seed):
+def _rect_state(ni, nj, bc, seed, **scheme):
     """A smooth positive state on a rectangular 2-D grid (density and pressure
     waves, a shear flow), guards by the boundary condition."""
     s0, _ = W.kelvin_helmholtz(8)
-    s = s0.with_(shape=(ni, nj, 1), bc=bc)
+    s = s0.with_(shape=(ni, nj, 1), bc=bc, **scheme)
     x, y, _ = W.cell_centres(s)
     X, Y = x[..., 0], y[..., 0]
     rng = np.random.default_rng(seed)
@@ -231,24 +195,44 @@ def _rect_state(ni, nj, bc, seed):
     return s, W.apply_bc_numpy(s, P)
 
 
+# grids of at least 2^19 zones (the pipelined form's threshold): square and
+# rectangular, partial last tile columns and rows (1058 = 33 x 32 + 2, 498 =
+# 31 x 16 + 2, 830, 3000), few tile rows (176 = 11 x 16), 2048^2
+PIPELINED = [(736, 736, "periodic", "plm", "hllc", 2), (740, 740, "outflow", "plm", "hlle", 3),
+             (726, 726, "reflecting", "pcm", "hllc", 1), (1058, 498, "periodic", "pcm", "hlle", 1),
+             (2048, 256, "periodic", "plm", "hllc", 2), (640, 830, "outflow", "plm", "hllc", 2),
+             (3000, 176, "reflecting", "plm", "hlle", 2), (2048, 2048, "periodic", "plm", "hllc", 2)]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("ni,nj,bc", [(256, 96, "periodic"), (160, 418, "outflow"), (1000, 34, "reflecting"),
-                                      (2048, 2048, "periodic")])
-def test_pipelined_host_step_rectangular(gpu_lib, ni, nj, bc):
-    """The pipelined host step on grids that are not square (a partial last
-    tile row and column, few tile rows, a large grid): the same bits as the
-    unpipelined path."""
+@pytest.mark.parametrize("ni,nj,bc,recon,riemann,rk", PIPELINED)
+def test_pipelined_host_step_matches_unpipelined(gpu_lib, ni, nj, bc, recon, riemann, rk):
+    """The drop-in call on a page-locked 2-D array runs as one launch that
+    pipelines the transfers in, the stages and the transfers out by bands of
+    host rows; a pageable array takes the unpipelined path (whole-grid
+    transfers, then the stages).  Several calls in a row (the rotation
+    parity of RK1 alternates), then a resident step: the same bits in the
+    host array and on the device, and the same Courant step."""
     import torch
-    s, P = _rect_state(ni, nj, bc, seed=ni + nj)
+    s, P = _rect_state(ni, nj, bc, seed=ni + nj, recon=recon, riemann=riemann, rk_order=rk, guard=2)
     with Solver(s, "mixed") as a, Solver(s, "mixed") as b:
         a.upload(P.copy())
         dt = a.courant() * s.cfl
         ref = P.copy()
         pin = torch.from_numpy(P.copy()).pin_memory()
-        for _ in range(2):
+        for _ in range(3):
             a.advance_host(ref, dt)
+            launches = b.stats().kernel_launches
             assert b.advance_host_ptr(pin.data_ptr(), dt) == 0
-        assert np.array_equal(pin.numpy().view(np.uint64), ref.view(np.uint64))
+            # the pipelined form: status reset, step start, the one launch
+            assert b.stats().kernel_launches - launches == 3
+            assert np.array_equal(pin.numpy().view(np.uint64), ref.view(np.uint64))
+        assert a.courant() == b.courant()
+        assert a.stats().steps == b.stats().steps
+        # the device state after the pipelined call continues like the other
+        a.advance(dt)
+        b.advance(dt)
+        assert np.array_equal(a.download().view(np.uint64), b.download().view(np.uint64))
 
 
 @pytest.mark.gpu
@@ -257,7 +241,7 @@ def test_host_register_makes_an_array_page_locked(gpu_lib):
     pinHostState): advance_host then reads and writes it in place, with the
     bits of the pageable path."""
     from mara2_gb300 import _native as N
-    s, P = W.kelvin_helmholtz(256)
+    s, P = W.kelvin_helmholtz(768)
     lib = N.load()
     with Solver(s, "mixed") as a, Solver(s, "mixed") as b:
         a.upload(P.copy())
