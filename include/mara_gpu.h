@@ -134,9 +134,10 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt);
 /* The drop-in form of advance: P_aos (host) in, advanced P_aos out, as
  * SolutionScheme::advance(MeshData&, t0, dt) does on MeshData::P.  Copies in,
  * advances, copies back and synchronises.  On a page-locked array of a 2-D
- * mixed-precision hydro grid (PCM / PLM, at least 128 zones along x) the
- * transfers in, the RK stages and the transfers out are pipelined in one
- * launch; the array receives the same bits as upload + advance + download. */
+ * mixed-precision hydro grid (PCM / PLM, at least 128 zones along x and
+ * 2^19 zones in all) the transfers in, the RK stages and the transfers out
+ * are pipelined in one launch; the array receives the same bits as upload +
+ * advance + download. */
 int mara_gpu_advance_host(MaraGpuHandle* h, double* P_aos, double t0, double dt);
 
 /* FieldOperator::getCourantTimestep (FieldOperator.cpp:125-169) with
