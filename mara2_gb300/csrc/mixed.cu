@@ -36,6 +36,8 @@ struct GridF {
     int weno_is;
     double gamma_d, pfloor_d;
     double gm1_d, inv_gm1_d;
+    float rm_gamf_hi, rm_gamf_lo;  // (gamma - 1) / gamma as an FP32 pair
+    float rm_hcoef;                // gamma / (gamma - 1)
 };
 
 template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 1 : RECON == RECON_PLM ? 2 : 3; };
@@ -218,8 +220,125 @@ __device__ __forceinline__ int rm_anton2dzw_rcp(const C2pRmhd& s, double* P)
     return rm_reconstruct_rcp(s, Z, W, iZ, iW, P);
 }
 
-// primitive recovery of the mixed path: FP32 for hydro and MHD, FP64
-// ConsToPrimRMHD for RMHD (the Newton iteration keeps FP64)
+// The same (Z, W) Newton iteration with its residuals f0, f1 formed in FP32
+// pairs (about 46 significant bits; FP64 runs at 1/64 of the FP32 rate on
+// this GPU) and the 2x2 Jacobian solved in FP32: an approximate Jacobian
+// keeps Newton's iteration converging (at rate ~1e-7 once quadratic
+// convergence has done its work), and the root is as accurate as the
+// residuals.  The reference's start, clamps, convergence test (|dZ/Z| +
+// |dW/W| <= 1e-12) and reconstruction (ConsToPrimRMHD.cpp:110-145, 183-255).
+// Returns false, leaving P untouched, wherever the pair form cannot be
+// trusted to finish as the FP64 iteration would: magnitudes outside
+// RM_PAIR_LO..RM_PAIR_HI (the pair's lower word would leave FP32's normal
+// range), no convergence within RM_PAIR_MAXIT iterations, a non-finite step,
+// or primitives that fail the reference's checks; the caller then runs the
+// FP64 solve, which also supplies the reference's error code.
+constexpr float RM_PAIR_LO = 1e-8f, RM_PAIR_HI = 1e8f, RM_PAIR_WMAX = 1e4f;
+constexpr int RM_PAIR_MAXIT = 16;
+
+__device__ __forceinline__ bool rm_in_range(df x) { return x.hi >= RM_PAIR_LO && x.hi <= RM_PAIR_HI; }
+
+__device__ __forceinline__ bool rm_recover_pair(const GridF& G, const df* U, const float* Pprev, float* Pout)
+{
+    const df D = U[0], Tau = U[4];
+    if (!rm_in_range(D) || !(Tau.hi >= 0.0f && Tau.hi <= RM_PAIR_HI)) return false;
+#pragma unroll
+    for (int q = 1; q < 8; ++q)
+        if (!(fabsf(U[q].hi) <= RM_PAIR_HI)) return false;
+    const df S2 = df_add(df_add(df_mul(U[1], U[1]), df_mul(U[2], U[2])), df_mul(U[3], U[3]));
+    const df B2 = df_add(df_add(df_mul(U[5], U[5]), df_mul(U[6], U[6])), df_mul(U[7], U[7]));
+    const df BS = df_add(df_add(df_mul(U[5], U[1]), df_mul(U[6], U[2])), df_mul(U[7], U[3]));
+    const df BS2 = df_mul(BS, BS);
+    const df gamf = {G.rm_gamf_hi, G.rm_gamf_lo};
+    const df iD = df_rcp(D);
+    df Z, W;
+    bool warm = false;
+    if (Pprev) {
+        // warm start from the zone's previous primitives (as the FP64 solve)
+        const float rho = Pprev[0], pre = Pprev[4];
+        const df V2 = df_add(df_add(two_prod(Pprev[1], Pprev[1]), two_prod(Pprev[2], Pprev[2])),
+                             two_prod(Pprev[3], Pprev[3]));
+        if (rho > 0.0f && pre > 0.0f && V2.hi < 1.0f) {
+            const df W2 = df_rcp(df_add_f(df_neg(V2), 1.0f));
+            const float h = 1.0f + pre * rcp_approx(rho) * G.rm_hcoef;
+            Z = df_mul_f(W2, rho * h);
+            W = df_sqrt(W2);
+            warm = true;
+        }
+    }
+    if (!warm) {  // the cold start of ConsToPrimRMHD::estimate_from_cons
+        Z = df_sqrt(df_add(S2, df_mul(D, D)));
+        W = df_mul(Z, iD);
+    }
+    if (!rm_in_range(Z) || !(W.hi >= 0.5f && W.hi <= RM_PAIR_WMAX)) return false;
+    const df hB2 = df_pow2(B2, 0.5f), hBS2 = df_pow2(BS2, 0.5f);
+    df iZ = df_rcp(Z), iW = df_rcp(W);
+    float error = 1.0f;
+    int it = 0;
+    while (error > 1e-12f) {
+        if (++it > RM_PAIR_MAXIT) return false;
+        const df W2 = df_mul(W, W), W2m1 = df_add_f(W2, -1.0f);
+        const df iW2 = df_mul(iW, iW), iZ2 = df_mul(iZ, iZ);
+        const df BZ = df_add(B2, Z);
+        // f0 = -S2 + (Z + B2)^2 (W^2 - 1) / W^2 - (2 Z + B2) BS2 / Z^2
+        const df f0 = df_sub(df_mul(df_mul(df_mul(BZ, BZ), W2m1), iW2),
+                             df_add(S2, df_mul(df_mul(df_add(df_pow2(Z, 2.0f), B2), BS2), iZ2)));
+        // f1 = -Tau + Z + B2 - Pre - B2 / (2 W^2) - BS2 / (2 Z^2) - D,
+        // Pre = (D / W) (Z / (D W) - 1) gamf
+        const df Pre = df_mul(df_mul(D, iW), df_mul(df_add_f(df_mul(df_mul(Z, iD), iW), -1.0f), gamf));
+        df f1 = df_sub(df_sub(Z, D), Tau);
+        f1 = df_sub(df_add(f1, B2), Pre);
+        f1 = df_sub(df_sub(f1, df_mul(hB2, iW2)), df_mul(hBS2, iZ2));
+        // the Jacobian, in FP32
+        const float z = Z.hi, w = W.hi, iz = iZ.hi, iw = iW.hi, g = gamf.hi;
+        const float bz = BZ.hi, iw2 = iw * iw, iw3 = iw2 * iw, iz3 = iz * iz * iz, z3 = z * z * z;
+        const float j00 = 2.0f * bz * (BS2.hi * W2.hi + W2m1.hi * z3) * iw2 * iz3;
+        const float j01 = 2.0f * bz * bz * iw3;
+        const float j10 = 1.0f + BS2.hi * iz3 - g * iw2;
+        const float j11 = B2.hi * iw3 + (2.0f * z - D.hi * w) * iw3 * g;
+        const float idet = rcp_approx(j00 * j11 - j01 * j10);
+        const float dZ = -(j11 * f0.hi - j01 * f1.hi) * idet;
+        const float dW = -(j00 * f1.hi - j10 * f0.hi) * idet;
+        if (!isfinite(dZ) || !isfinite(dW)) return false;
+        df Zn = df_add_f(Z, dZ), Wn = df_add_f(W, dW);
+        if (Zn.hi < 0.0f) Zn = df_neg(Zn);
+        if (Wn.hi < 1.0f || (Wn.hi == 1.0f && Wn.lo < 0.0f)) Wn = {1.0f, 0.0f};
+        if (!rm_in_range(Zn) || Wn.hi > RM_PAIR_WMAX) return false;
+        Z = Zn;
+        W = Wn;
+        iZ = df_rcp(Z);
+        iW = df_rcp(W);
+        error = fabsf(dZ * iZ.hi) + fabsf(dW * iW.hi);
+    }
+    // reconstruction, checked as ConsToPrimRMHD::check_prim does
+    const df iZB = df_rcp(df_add(Z, B2));
+    const df b0 = df_mul(df_mul(BS, W), iZ);
+    const df rho = df_mul(D, iW);
+    df pre = df_mul(df_mul(rho, df_add_f(df_mul(df_mul(Z, iW), iD), -1.0f)), gamf);
+    if (pre.hi <= 0.0f && G.pressure_floor > 0.0f) pre = df_mul_f(rho, G.pressure_floor);
+    df v[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) v[a] = df_mul(df_add(U[1 + a], df_mul(df_mul(b0, U[5 + a]), iW)), iZB);
+    const df v2 = df_add(df_add(df_mul(v[0], v[0]), df_mul(v[1], v[1])), df_mul(v[2], v[2]));
+    if (!(v2.hi < 1.0f) || pre.hi < 0.0f || rho.hi < 0.0f) return false;
+    float P[8];
+    P[0] = __fadd_rn(rho.hi, rho.lo);
+    P[1] = __fadd_rn(v[0].hi, v[0].lo);
+    P[2] = __fadd_rn(v[1].hi, v[1].lo);
+    P[3] = __fadd_rn(v[2].hi, v[2].lo);
+    P[4] = __fadd_rn(pre.hi, pre.lo);
+#pragma unroll
+    for (int q = 5; q < 8; ++q) P[q] = __fadd_rn(U[q].hi, U[q].lo);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (!isfinite(P[q])) return false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Pout[q] = P[q];
+    return true;
+}
+
+// primitive recovery of the mixed path: FP32 for hydro and MHD; for RMHD the
+// pair-residual Newton iteration above, else the FP64 ConsToPrimRMHD solve
 template <int LAW>
 __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code, const float* Pprev = nullptr)
 {
@@ -238,6 +357,7 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
         *code = e;
         return e;
     } else {
+        if (rm_recover_pair(G, Un, Pprev, P)) return ST_OK;
         double U[NQ], Pd[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; ++q) U[q] = df_to_double(Un[q]);
@@ -591,6 +711,12 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
     F.pressure_floor = (float) c->pressure_floor; F.weno_is = c->weno_is;
     F.gamma_d = c->gamma; F.pfloor_d = c->pressure_floor;
     F.gm1_d = c->gamma - 1.0; F.inv_gm1_d = 1.0 / (c->gamma - 1.0);
+    {
+        const double gamf = (c->gamma - 1.0) / c->gamma;
+        F.rm_gamf_hi = (float) gamf;
+        F.rm_gamf_lo = (float) (gamf - (double) F.rm_gamf_hi);
+        F.rm_hcoef = (float) (c->gamma / (c->gamma - 1.0));
+    }
     m->pp.gamma = c->gamma; m->pp.plm_theta = c->plm_theta; m->pp.shenzha_A = c->shenzha_A;
     m->pp.pressure_floor = c->pressure_floor; m->pp.weno_is = c->weno_is;
 

@@ -4,9 +4,11 @@
 // run in FP32 (mixed.cu is compiled with approximate FP32 division and
 // square root and flush-to-zero); the conserved-state accumulator is an
 // unevaluated FP32 pair (hi + lo, about 48 significant bits) updated with
-// error-free transformations (Knuth's TwoSum, FMA-based TwoProd); the
-// relativistic primitive recovery runs its Newton iterations in FP64 (the
-// same routines as the plain path).  The formulas are those of the reference
+// error-free transformations (Knuth's TwoSum, FMA-based TwoProd; pair
+// arithmetic after Dekker 1971 and the double-double library of Hida, Li and
+// Bailey); the relativistic primitive recovery forms its Newton residuals in
+// that pair arithmetic and falls back to FP64 (the plain path's routines)
+// where the pair iteration cannot finish.  The formulas are those of the reference
 // routines named beside each function; only the operation order and the
 // precision differ.
 #pragma once
@@ -58,6 +60,64 @@ __device__ __forceinline__ df df_mul_f(df a, float b)
     float e = __fmaf_rn(a.hi, b, -p);
     e = __fmaf_rn(a.lo, b, e);
     return fast_two_sum(p, e);
+}
+
+// hardware approximations (about one unit in the last place), the seeds of
+// the pair reciprocal and square root below
+__device__ __forceinline__ float rcp_approx(float a)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+__device__ __forceinline__ float sqrt_approx(float a)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+// exact product of two floats as a pair (FMA-based TwoProd)
+__device__ __forceinline__ df two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// pair x pair (Dekker's product with FMA; about 2^-47 relative)
+__device__ __forceinline__ df df_mul(df a, df b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+// multiplication by a power of two: exact on both words
+__device__ __forceinline__ df df_pow2(df a, float p) { return {__fmul_rn(a.hi, p), __fmul_rn(a.lo, p)}; }
+
+// 1 / a: one Newton-Raphson step r + r (1 - a r) on the hardware seed, the
+// residual 1 - a r formed from the exact pair product (1 - (a r).hi is exact
+// by Sterbenz's lemma); about 2^-46 relative
+__device__ __forceinline__ df df_rcp(df a)
+{
+    const float r = rcp_approx(a.hi);
+    const df p = df_mul_f(a, r);
+    const float e = __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo);
+    return fast_two_sum(r, __fmul_rn(r, e));
+}
+
+// sqrt(a) for a > 0: one Newton step s + (a - s^2) / (2 s) on the seed
+__device__ __forceinline__ df df_sqrt(df a)
+{
+    const float s = sqrt_approx(a.hi);
+    const df s2 = two_prod(s, s);
+    const float d = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, s2.hi), s2.lo), a.lo);
+    return fast_two_sum(s, __fmul_rn(d, __fmul_rn(0.5f, rcp_approx(s))));
 }
 
 __device__ __forceinline__ df df_from_double(double x)
