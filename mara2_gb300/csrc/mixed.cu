@@ -11,6 +11,7 @@
 //    primitive recovery (FP32 for hydro and MHD, FP64 Newton for RMHD), and
 //    writing FP32 primitives with their guard images for the next sweep.
 #include <algorithm>
+#include <type_traits>
 #include <cfloat>
 #include <cstring>
 #include <vector>
@@ -42,11 +43,15 @@ struct GridF {
 
 template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 1 : RECON == RECON_PLM ? 2 : 3; };
 
-template <int LAW, int RECON, int RIEMANN>
+// The face fluxes along one axis of the general form.  AXIS >= 0 is the
+// axis at compile time (no multiplications by the zero components of the
+// normal); AXIS < 0 takes it, and the normal, at run time.
+template <int LAW, int RECON, int RIEMANN, int AXIS>
 __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P, float* __restrict__ F, GridF G,
                                                      int axis, int lo0, int lo1, int lo2, int nb0,
                                                      const int* __restrict__ done, DevStatus* st)
 {
+    if constexpr (AXIS >= 0) axis = AXIS;
     constexpr int NQ = LawInfo<LAW>::NQ;
     constexpr int S = SOf<RECON>::S;
     if (*done || st->code) return;
@@ -56,7 +61,6 @@ __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P
     const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
     const long long stride = axis == 0 ? 1 : axis == 1 ? (long long) G.N[0] : (long long) G.N[0] * G.N[1];
     const long long base = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    const float n[3] = {G.nrm[axis][0], G.nrm[axis][1], G.nrm[axis][2]};
     float PL[NQ], PR[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
@@ -72,6 +76,9 @@ __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P
             PR[q] = weno5_f<false>(&v[3], G.weno_is, G.shenzha_A);
         }
     }
+    using Normal = std::conditional_t<(AXIS >= 0), AxisNormal<(AXIS >= 0 ? AXIS : 0)>, VecNormal>;
+    Normal n;
+    if constexpr (AXIS < 0) n.n = G.nrm[axis];
     StateF<NQ> L, R;
     int e = law_prim_f<LAW>(G.gamma, PL, n, L);
     if (e == ST_OK) e = law_prim_f<LAW>(G.gamma, PR, n, R);
@@ -409,52 +416,92 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
     }
 }
 
+// Courant step of one zone from its FP32 primitives: lmin / the largest
+// |eigenvalue| over the three face normals (FieldOperator::getCourantTimestep,
+// FieldOperator.cpp:125-169); an eigenvalue error goes to the status
 template <int LAW>
-__global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, float* const* Uh, float* const* Ul,
-                                                       int s_buf, int src, int dst, FluxViewF V, GridF G,
+__device__ __forceinline__ float zone_dt_f(const GridF& G, const float* P, DevStatus* st)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    float lmax = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        StateF<NQ> S;
+        const int e = law_prim_f<LAW>(G.gamma, P, VecNormal{G.nrm[a]}, S);
+        if (e != ST_OK) { atomicCAS(&st->code, 0, e); return 3.0e38f; }
+        lmax = fmaxf(lmax, fmaxf(fabsf(S.amax), fabsf(S.amin)));
+    }
+    return G.lmin / lmax;
+}
+
+// One RK stage's update of the general form: divergence of the (flux-CT
+// corrected) face fluxes, the RK combine on FP32 pairs, the primitive
+// recovery, the primitives with their guard images, and on the last stage
+// (cfl not null) the zone's Courant step.  Every load of a zone comes before
+// its first store, so the loads of all fields are in flight together (the
+// stage input and output may be one array, RK1).
+template <int LAW>
+__global__ void __launch_bounds__(128) update_f_kernel(float* __restrict__ Pf, const float* U0h, const float* U0l,
+                                                       const float* Uph, const float* Upl, float* Unh, float* Unl,
+                                                       FluxViewF V, GridF G,
                                                        const double* __restrict__ dtp, float b, float omb,
-                                                       const int* __restrict__ done, DevStatus* st)
+                                                       const int* __restrict__ done, DevStatus* st,
+                                                       unsigned long long* cfl)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     if (*done || st->code || st->halt) return;
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ii >= G.n[0]) return;
+    const bool active = ii < G.n[0];
     const int jj = blockIdx.y, kk = blockIdx.z;
     const int i = ii + G.g[0], j = jj + G.g[1], k = kk + G.g[2];
     const long long uc = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
-    const float dt = (float) *dtp;
-    const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
-    df Un[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        float L = 0.f;
-        if (fx) L -= (face_flux_f<NQ>(V, G, 0, q, i + 1, j, k) - face_flux_f<NQ>(V, G, 0, q, i, j, k)) * G.idx[0];
-        if (fy) L -= (face_flux_f<NQ>(V, G, 1, q, i, j + 1, k) - face_flux_f<NQ>(V, G, 1, q, i, j, k)) * G.idx[1];
-        if (fz) L -= (face_flux_f<NQ>(V, G, 2, q, i, j, k + 1) - face_flux_f<NQ>(V, G, 2, q, i, j, k)) * G.idx[2];
-        const df U0 = {Uh[s_buf][q * G.sU + uc], Ul[s_buf][q * G.sU + uc]};
-        const df Up = {Uh[src][q * G.sU + uc], Ul[src][q * G.sU + uc]};
-        Un[q] = rk_combine(U0, Up, dt * L, b, omb);
-        Uh[dst][q * G.sU + uc] = Un[q].hi;
-        Ul[dst][q * G.sU + uc] = Un[q].lo;
-    }
-    float Pn[NQ];
-    int code = ST_OK;
     const long long pc = ((long long) k * G.N[1] + j) * G.N[0] + i;
-    // the zone's previous primitives: the RMHD recovery's starting point, and
-    // what a failed recovery keeps (read only then for the other laws)
-    float Pold[NQ];
-    if constexpr (LAW == LAW_RMHD)
+    float Pn[NQ];
+    float zdt = 3.0e38f;
+    if (active) {
+        const float dt = (float) *dtp;
+        const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
+        df U0[NQ], Up[NQ];
+        float L[NQ];
+        // the zone's previous primitives: the RMHD recovery's starting point,
+        // and what a failed recovery keeps (read only then for the other laws)
+        float Pold[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Pold[q] = Pf[q * G.sP + pc];
-    const int e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
-    if (e == ST_INVERSION_FAILURE) {
-        atomicAdd(&st->failures, 1);
-        const unsigned long long z = (unsigned long long) uc;
-        const unsigned long long prev = atomicMin(&st->first_zone, z);
-        if (z < prev) atomicExch(&st->first_code, code);
+        for (int q = 0; q < NQ; ++q) {
+            U0[q] = {U0h[q * G.sU + uc], U0l[q * G.sU + uc]};
+            Up[q] = {Uph[q * G.sU + uc], Upl[q * G.sU + uc]};
+            if constexpr (LAW == LAW_RMHD) Pold[q] = Pf[q * G.sP + pc];
+        }
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Pn[q] = LAW == LAW_RMHD ? Pold[q] : Pf[q * G.sP + pc];
+        for (int q = 0; q < NQ; ++q) {
+            float l = 0.f;
+            if (fx) l -= (face_flux_f<NQ>(V, G, 0, q, i + 1, j, k) - face_flux_f<NQ>(V, G, 0, q, i, j, k)) * G.idx[0];
+            if (fy) l -= (face_flux_f<NQ>(V, G, 1, q, i, j + 1, k) - face_flux_f<NQ>(V, G, 1, q, i, j, k)) * G.idx[1];
+            if (fz) l -= (face_flux_f<NQ>(V, G, 2, q, i, j, k + 1) - face_flux_f<NQ>(V, G, 2, q, i, j, k)) * G.idx[2];
+            L[q] = l;
+        }
+        df Un[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) Un[q] = rk_combine(U0[q], Up[q], dt * L[q], b, omb);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            Unh[q * G.sU + uc] = Un[q].hi;
+            Unl[q * G.sU + uc] = Un[q].lo;
+        }
+        int code = ST_OK;
+        const int e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
+        if (e == ST_INVERSION_FAILURE) {
+            atomicAdd(&st->failures, 1);
+            const unsigned long long z = (unsigned long long) uc;
+            const unsigned long long prev = atomicMin(&st->first_zone, z);
+            if (z < prev) atomicExch(&st->first_code, code);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) Pn[q] = LAW == LAW_RMHD ? Pold[q] : Pf[q * G.sP + pc];
+        }
+        if (cfl) zdt = zone_dt_f<LAW>(G, Pn, st);
     }
+    // every lane of a warp reaches the reduction (cfl is the same for all)
+    if (cfl) block_min_to(cfl, zdt);
+    if (!active) return;
     // the zone's cell, then (zones within a guard width of an edge) its guard
     // images on every combination of axes
 #pragma unroll
@@ -499,7 +546,7 @@ __global__ void __launch_bounds__(256) courant_f_kernel(const float* __restrict_
         float lmax = 0.f;
         for (int a = 0; a < 3; ++a) {
             StateF<NQ> S;
-            const int e = law_prim_f<LAW>(G.gamma, P, G.nrm[a], S);
+            const int e = law_prim_f<LAW>(G.gamma, P, VecNormal{G.nrm[a]}, S);
             if (e != ST_OK) { atomicCAS(&st->code, 0, e); break; }
             lmax = fmaxf(lmax, fmaxf(fabsf(S.amax), fabsf(S.amin)));
         }
@@ -620,6 +667,13 @@ __global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, cons
 __global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long long) __double_as_longlong(DBL_MAX); }
 __global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
 __global__ void k_rot_flip(int* rot) { *rot ^= 1; }
+// the general form's last stage reduced the new state's Courant step into
+// next; it becomes the handle's only if the step ran (a step not taken, at
+// t_final or after an error, leaves the previous state's step)
+__global__ void k_cfl_commit(unsigned long long* bits, const unsigned long long* next, const DevStatus* st)
+{
+    if (!st->done && !st->code && !st->halt) *bits = *next;
+}
 
 // Start of one driver-loop step of the fused path, in one thread: the Courant
 // step that the previous step's last stage (or the load) reduced becomes the
@@ -660,8 +714,6 @@ struct MixedState {
     bool fused = false;
     float* Uh[3] = {nullptr, nullptr, nullptr};
     float* Ul[3] = {nullptr, nullptr, nullptr};
-    float** dUh = nullptr;  // device copies of the pointer tables
-    float** dUl = nullptr;
     float* Pf = nullptr;
     float* F[3] = {nullptr, nullptr, nullptr};
     float* E[3] = {nullptr, nullptr, nullptr};  // flux-CT edge EMFs (magnetic laws)
@@ -672,6 +724,7 @@ struct MixedState {
     int* drot = nullptr;     // state buffer index (device)
     int rot = 0;             // host mirror for the general form's parity
     unsigned long long* dcfl = nullptr;
+    unsigned long long* dcfl_next = nullptr;  // general form: the last stage's Courant reduction
     int tx = 32, ty = 16;
     int ctas = 0;
     int timing = 0;
@@ -727,16 +780,11 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
         rc = dev_alloc((void**) &m->Uh[b], sizeof(float) * G.sU * nq, s, bytes);
         if (!rc) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
     }
-    if (!rc) rc = dev_alloc((void**) &m->dUh, sizeof(float*) * 3, s, bytes);
-    if (!rc) rc = dev_alloc((void**) &m->dUl, sizeof(float*) * 3, s, bytes);
     if (!rc) rc = dev_alloc((void**) &m->drot, sizeof(int), s, bytes);
     if (!rc) rc = dev_alloc((void**) &m->dcfl, sizeof(unsigned long long), s, bytes);
-    if (!rc) {
-        cudaMemcpyAsync(m->dUh, m->Uh, sizeof(float*) * 3, cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(m->dUl, m->Ul, sizeof(float*) * 3, cudaMemcpyHostToDevice, s);
-    }
     if (!rc && !m->fused) {
         rc = dev_alloc((void**) &m->Pf, sizeof(float) * G.sP * nq, s, bytes);
+        if (!rc) rc = dev_alloc((void**) &m->dcfl_next, sizeof(unsigned long long), s, bytes);
         for (int a = 0; a < 3 && !rc; ++a)
             if (G.n[a] > 1) rc = dev_alloc((void**) &m->F[a], sizeof(float) * G.sF * nq, s, bytes);
         if (G.ct && nq == 8)
@@ -785,7 +833,7 @@ void mixed_destroy(MixedState* m)
     if (!m) return;
     for (auto& e : m->ev) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
     for (int b = 0; b < 3; ++b) { cudaFree(m->Uh[b]); cudaFree(m->Ul[b]); }
-    cudaFree(m->dUh); cudaFree(m->dUl); cudaFree(m->drot); cudaFree(m->dcfl);
+    cudaFree(m->drot); cudaFree(m->dcfl); cudaFree(m->dcfl_next);
     cudaFree(m->Pf);
     for (int a = 0; a < 3; ++a) cudaFree(m->F[a]);
     for (int e = 0; e < 3; ++e) cudaFree(m->E[e]);
@@ -928,7 +976,19 @@ static void flux_f_launch(MixedState* m, int axis, const int* done, DevStatus* s
         else { lo[a] = 0; nb[a] = 1; }
     }
     dim3 grid((nb[0] + 127) / 128, nb[1], nb[2]);
-    flux_f_kernel<LAW, RECON, RIEMANN><<<grid, 128, 0, s>>>(m->Pf, m->F[axis], G, axis, lo[0], lo[1], lo[2], nb[0], done, st);
+#define MARA_FLUX_ARGS m->Pf, m->F[axis], G, axis, lo[0], lo[1], lo[2], nb[0], done, st
+    // hydro and MHD fluxes take the axis at compile time; the relativistic
+    // law's cost is its quartic, so it keeps one kernel for all axes
+    if constexpr (LAW == LAW_RMHD) {
+        flux_f_kernel<LAW, RECON, RIEMANN, -1><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS);
+    } else {
+        switch (axis) {
+            case 0: flux_f_kernel<LAW, RECON, RIEMANN, 0><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
+            case 1: flux_f_kernel<LAW, RECON, RIEMANN, 1><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
+            default: flux_f_kernel<LAW, RECON, RIEMANN, 2><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
+        }
+    }
+#undef MARA_FLUX_ARGS
 }
 
 template <int LAW, int RECON>
@@ -982,18 +1042,22 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
         const float b = B_TAB[order - 1][rk];
         const int src = rk == 0 ? sb : tb;
         const int dst = rk == order - 1 ? sb : tb;
+        const bool last = rk == order - 1;
+        // the last stage also reduces the new state's Courant step
+        if (last) k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl_next);
+        unsigned long long* cfl = last ? m->dcfl_next : nullptr;
         dim3 grid((m->G.n[0] + 127) / 128, m->G.n[1], m->G.n[2]);
         timed(m, s, [&] {
+#define MARA_UPDATE_ARGS m->Pf, m->Uh[sb], m->Ul[sb], m->Uh[src], m->Ul[src], m->Uh[dst], m->Ul[dst], V, m->GF, dt, b, 1.f - b, done, st, cfl
             switch (m->cfg.law) {
-                case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
-                case MARA_LAW_MHD: update_f_kernel<LAW_MHD><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
-                default: update_f_kernel<LAW_RMHD><<<grid, 128, 0, s>>>(m->Pf, m->dUh, m->dUl, sb, src, dst, V, m->GF, dt, b, 1.f - b, done, st); break;
+                case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                case MARA_LAW_MHD: update_f_kernel<LAW_MHD><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                default: update_f_kernel<LAW_RMHD><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
             }
+#undef MARA_UPDATE_ARGS
         });
     }
-    // Courant step of the new state for the next step
-    k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
-    courant_general(m, st, s);
+    k_cfl_commit<<<1, 1, 0, s>>>(m->dcfl, m->dcfl_next, st);
 }
 
 // ---- fused hydro tiles ------------------------------------------------------
@@ -1517,9 +1581,11 @@ int mixed_launches_per_step(const MixedState* m)
 {
     // fused: the step-begin kernel, one launch per stage, the RK1 rotation
     if (m->fused) return 1 + m->cfg.rk_order + (m->cfg.rk_order == 1 ? 1 : 0);
+    // general: per stage the flux launches, the edge EMFs (flux CT), the
+    // update; per step the Courant slot's reset and commit
     int axes = 0;
     for (int a = 0; a < 3; ++a) axes += m->G.n[a] > 1;
-    return m->cfg.rk_order * (axes + 1) + 2;
+    return m->cfg.rk_order * (axes + 1 + (m->E[0] ? 1 : 0)) + 2;
 }
 
 void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s) { k_cfl_publish<<<1, 1, 0, s>>>(m->dcfl, st); }

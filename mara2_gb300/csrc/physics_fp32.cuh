@@ -212,13 +212,28 @@ template <int NQ> struct StateF {
     float amax, amin;  // max / min eigenvalue over the reference's 10 slots
 };
 
+// A face normal: a coordinate axis fixed at compile time (the Cartesian
+// faces of the flux kernels; the 6e-17 x-component of the reference's yhat
+// lies far below FP32 rounding) or a general unit vector.  add(d, x, t) is
+// x + t n_d, without the multiplications by zero of an axis.
+template <int AXIS> struct AxisNormal {
+    __device__ __forceinline__ float dot(float x, float y, float z) const { return AXIS == 0 ? x : AXIS == 1 ? y : z; }
+    __device__ __forceinline__ float add(int d, float x, float t) const { return d == AXIS ? x + t : x; }
+};
+struct VecNormal {
+    const float* n;
+    __device__ __forceinline__ float dot(float x, float y, float z) const { return x * n[0] + y * n[1] + z * n[2]; }
+    __device__ __forceinline__ float add(int d, float x, float t) const { return x + t * n[d]; }
+};
+
 // NewtonianHydro::fromPrimitive (ConservationLaws.cpp:253-290)
-__device__ __forceinline__ void hydro_prim_f(float gamma, const float* P, const float* n, StateF<5>& S)
+template <class N>
+__device__ __forceinline__ void hydro_prim_f(float gamma, const float* P, const N& n, StateF<5>& S)
 {
     const float gm1 = gamma - 1.0f;
     const float cs = sqrtf(gamma * P[4] / P[0]);
     const float vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
-    const float vn = P[1] * n[0] + P[2] * n[1] + P[3] * n[2];
+    const float vn = n.dot(P[1], P[2], P[3]);
 #pragma unroll
     for (int q = 0; q < 5; ++q) S.P[q] = P[q];
     S.U[0] = P[0];
@@ -227,9 +242,9 @@ __device__ __forceinline__ void hydro_prim_f(float gamma, const float* P, const 
     S.U[3] = P[0] * P[3];
     S.U[4] = 0.5f * P[0] * vv + P[4] / gm1;
     S.F[0] = vn * S.U[0];
-    S.F[1] = vn * S.U[1] + P[4] * n[0];
-    S.F[2] = vn * S.U[2] + P[4] * n[1];
-    S.F[3] = vn * S.U[3] + P[4] * n[2];
+    S.F[1] = n.add(0, vn * S.U[1], P[4]);
+    S.F[2] = n.add(1, vn * S.U[2], P[4]);
+    S.F[3] = n.add(2, vn * S.U[3], P[4]);
     S.F[4] = vn * (S.U[4] + P[4]);
     S.amax = fmaxf(vn + cs, 0.0f);
     S.amin = fminf(vn - cs, 0.0f);
@@ -247,7 +262,8 @@ __device__ __forceinline__ void hydro_cons_f(float gamma, const float* U, float*
 }
 
 // NewtonianMHD::fromPrimitive (ConservationLaws.cpp:416-487)
-__device__ __forceinline__ void mhd_prim_f(float gamma, const float* P, const float* n, StateF<8>& S)
+template <class N>
+__device__ __forceinline__ void mhd_prim_f(float gamma, const float* P, const N& n, StateF<8>& S)
 {
     const float gm1 = gamma - 1.0f;
     const float ir = 1.0f / P[0];
@@ -255,8 +271,8 @@ __device__ __forceinline__ void mhd_prim_f(float gamma, const float* P, const fl
     const float vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
     const float BB = P[5] * P[5] + P[6] * P[6] + P[7] * P[7];
     const float Bv = P[5] * P[1] + P[6] * P[2] + P[7] * P[3];
-    const float vn = P[1] * n[0] + P[2] * n[1] + P[3] * n[2];
-    const float Bn = P[5] * n[0] + P[6] * n[1] + P[7] * n[2];
+    const float vn = n.dot(P[1], P[2], P[3]);
+    const float Bn = n.dot(P[5], P[6], P[7]);
     const float ps = P[4] + 0.5f * BB;
 #pragma unroll
     for (int q = 0; q < 8; ++q) S.P[q] = P[q];
@@ -269,9 +285,9 @@ __device__ __forceinline__ void mhd_prim_f(float gamma, const float* P, const fl
     S.U[6] = P[6];
     S.U[7] = P[7];
     S.F[0] = vn * S.U[0];
-    S.F[1] = vn * S.U[1] - Bn * P[5] + ps * n[0];
-    S.F[2] = vn * S.U[2] - Bn * P[6] + ps * n[1];
-    S.F[3] = vn * S.U[3] - Bn * P[7] + ps * n[2];
+    S.F[1] = n.add(0, vn * S.U[1] - Bn * P[5], ps);
+    S.F[2] = n.add(1, vn * S.U[2] - Bn * P[6], ps);
+    S.F[3] = n.add(2, vn * S.U[3] - Bn * P[7], ps);
     S.F[4] = vn * (S.U[4] + ps) - Bn * Bv;
     S.F[5] = vn * S.U[5] - Bn * P[1];
     S.F[6] = vn * S.U[6] - Bn * P[2];
@@ -361,15 +377,16 @@ __device__ __forceinline__ int quartic_roots_f(float d4, float d3, float d2, flo
 // RelativisticMHD::fromPrimitive in FP32 (ConservationLaws.cpp:659-836).
 // The wave-speed extremes come from the quartic roots, the Alfven pair and
 // vn, as in the reference's eigenvalue table.
-__device__ __forceinline__ int rmhd_prim_f(float gamma, const float* P, const float* n, StateF<8>& S)
+template <class N>
+__device__ __forceinline__ int rmhd_prim_f(float gamma, const float* P, const N& n, StateF<8>& S)
 {
     const float gm1 = gamma - 1.0f;
     const float vv = P[1] * P[1] + P[2] * P[2] + P[3] * P[3];
     if (vv >= 1.f) return ST_SUPERLUMINAL;
     const float BB = P[5] * P[5] + P[6] * P[6] + P[7] * P[7];
     const float Bv = P[5] * P[1] + P[6] * P[2] + P[7] * P[3];
-    const float vn = P[1] * n[0] + P[2] * n[1] + P[3] * n[2];
-    const float Bn = P[5] * n[0] + P[6] * n[1] + P[7] * n[2];
+    const float vn = n.dot(P[1], P[2], P[3]);
+    const float Bn = n.dot(P[5], P[6], P[7]);
     const float W2 = 1.0f / (1.0f - vv);
     const float W0 = sqrtf(W2);
     const float iW0 = 1.0f / W0;
@@ -378,7 +395,7 @@ __device__ __forceinline__ int rmhd_prim_f(float gamma, const float* P, const fl
     const float b1 = (P[5] + b0 * W0 * P[1]) * iW0;
     const float b2 = (P[6] + b0 * W0 * P[2]) * iW0;
     const float b3 = (P[7] + b0 * W0 * P[3]) * iW0;
-    const float bn = b1 * n[0] + b2 * n[1] + b3 * n[2];
+    const float bn = n.dot(b1, b2, b3);
     const float ir = 1.0f / P[0];
     const float e0 = P[4] * ir / gm1;
     const float p0 = P[4];
@@ -397,9 +414,9 @@ __device__ __forceinline__ int rmhd_prim_f(float gamma, const float* P, const fl
     S.U[6] = P[6];
     S.U[7] = P[7];
     S.F[0] = vn * S.U[0];
-    S.F[1] = vn * S.U[1] - Bn * b1 * iW0 + ps * n[0];
-    S.F[2] = vn * S.U[2] - Bn * b2 * iW0 + ps * n[1];
-    S.F[3] = vn * S.U[3] - Bn * b3 * iW0 + ps * n[2];
+    S.F[1] = n.add(0, vn * S.U[1] - Bn * b1 * iW0, ps);
+    S.F[2] = n.add(1, vn * S.U[2] - Bn * b2 * iW0, ps);
+    S.F[3] = n.add(2, vn * S.U[3] - Bn * b3 * iW0, ps);
     S.F[4] = vn * S.U[4] - Bn * b0 * iW0 + ps * vn;
     S.F[5] = vn * S.U[5] - Bn * P[1];
     S.F[6] = vn * S.U[6] - Bn * P[2];
@@ -440,8 +457,8 @@ __device__ __forceinline__ int rmhd_prim_f(float gamma, const float* P, const fl
 }
 
 // ---------------------------------------------------------------------------
-template <int LAW>
-__device__ __forceinline__ int law_prim_f(float gamma, const float* P, const float* n, StateF<LawInfo<LAW>::NQ>& S)
+template <int LAW, class N>
+__device__ __forceinline__ int law_prim_f(float gamma, const float* P, const N& n, StateF<LawInfo<LAW>::NQ>& S)
 {
     if constexpr (LAW == LAW_HYDRO) { hydro_prim_f(gamma, P, n, S); return ST_OK; }
     else if constexpr (LAW == LAW_MHD) { mhd_prim_f(gamma, P, n, S); return ST_OK; }
@@ -462,15 +479,15 @@ __device__ __forceinline__ void hlle_f(const StateF<NQ>& L, const StateF<NQ>& R,
 }
 
 // HllcNewtonianHydroRiemannSolver::solve (RiemannSolvers.cpp:63-118)
-template <int NQ>
-__device__ __forceinline__ void hllc_f(const StateF<NQ>& L, const StateF<NQ>& R, const float* n, float* F)
+template <int NQ, class N>
+__device__ __forceinline__ void hllc_f(const StateF<NQ>& L, const StateF<NQ>& R, const N& n, float* F)
 {
     const float ap = fmaxf(L.amax, R.amax);
     const float am = fminf(L.amin, R.amin);
     const float* Pl = L.P;
     const float* Pr = R.P;
-    const float vnr = Pr[1] * n[0] + Pr[2] * n[1] + Pr[3] * n[2];
-    const float vnl = Pl[1] * n[0] + Pl[2] * n[1] + Pl[3] * n[2];
+    const float vnr = n.dot(Pr[1], Pr[2], Pr[3]);
+    const float vnl = n.dot(Pl[1], Pl[2], Pl[3]);
     const float ml = Pl[0] * (am - vnl), mr = Pr[0] * (ap - vnr);
     const float lc = ((Pr[4] - mr * vnr) - (Pl[4] - ml * vnl)) / (ml - mr);
 #pragma unroll
@@ -484,9 +501,9 @@ __device__ __forceinline__ void hllc_f(const StateF<NQ>& L, const StateF<NQ>& R,
         float Us[5];
         Us[0] = fl;
         Us[4] = fl * (L.U[4] * il + (lc - vnl) * (lc + Pl[4] / ml));
-        Us[1] = fl * ((lc - vnl) * n[0] + Pl[1]);
-        Us[2] = fl * ((lc - vnl) * n[1] + Pl[2]);
-        Us[3] = fl * ((lc - vnl) * n[2] + Pl[3]);
+        Us[1] = fl * n.add(0, Pl[1], lc - vnl);
+        Us[2] = fl * n.add(1, Pl[2], lc - vnl);
+        Us[3] = fl * n.add(2, Pl[3], lc - vnl);
 #pragma unroll
         for (int i = 0; i < 5; ++i) F[i] = L.F[i] + am * (Us[i] - L.U[i]);
     } else if (0.0f <= ap) {
@@ -495,9 +512,9 @@ __device__ __forceinline__ void hllc_f(const StateF<NQ>& L, const StateF<NQ>& R,
         float Us[5];
         Us[0] = fr;
         Us[4] = fr * (R.U[4] * ir + (lc - vnr) * (lc + Pr[4] / mr));
-        Us[1] = fr * ((lc - vnr) * n[0] + Pr[1]);
-        Us[2] = fr * ((lc - vnr) * n[1] + Pr[2]);
-        Us[3] = fr * ((lc - vnr) * n[2] + Pr[3]);
+        Us[1] = fr * n.add(0, Pr[1], lc - vnr);
+        Us[2] = fr * n.add(1, Pr[2], lc - vnr);
+        Us[3] = fr * n.add(2, Pr[3], lc - vnr);
 #pragma unroll
         for (int i = 0; i < 5; ++i) F[i] = R.F[i] + ap * (Us[i] - R.U[i]);
     } else {

@@ -32,14 +32,15 @@ def _cases():
     out.append(("mhd16cube-general-ct", s, P, 6))
     s, P = W.rmhd_blast(48)
     out.append(("rmhd48-general-weno5", s, P, 6))
-    # the same flow scaled self-similarly (rho, p by 1e-10, B by 1e-5): the
-    # conserved density falls below the FP32-pair recovery's range, so every
-    # zone takes the FP64 Newton solve instead
+    # a dense quadrant (rho 1e9, p 1e7) beside the blast: its conserved
+    # density lies above the FP32-pair recovery's range, so those zones take
+    # the FP64 Newton solve, the rest the pair iteration
+    x, y, _ = W.cell_centres(s)
+    dense = (x < -0.5) & (y < -0.5)
     Q = P.copy()
-    Q[..., 0] *= 1e-10
-    Q[..., 4] *= 1e-10
-    Q[..., 5:8] *= 1e-5
-    out.append(("rmhd48-scaled-fp64-recovery", s, Q, 6))
+    Q[..., 0] = np.where(dense, 1e9, Q[..., 0])
+    Q[..., 4] = np.where(dense, 1e7, Q[..., 4])
+    out.append(("rmhd48-dense-fp64-recovery", s, W.apply_bc_numpy(s, Q), 6))
     return out
 
 
@@ -165,3 +166,32 @@ def test_cluster_run_stops_at_t_final_and_continues(gpu_lib, port):
     assert n1 == 100 and abs((n1 + n2) - len(dts)) <= 2
     err = rel_l1(out[s.interior()], ref[s.interior()])
     assert err[0] < 1e-4, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make", [lambda: W.mhd_turbulence(16), lambda: W.rmhd_blast(32)], ids=["mhd", "rmhd"])
+def test_general_run_split_at_t_final_continues_identically(gpu_lib, make):
+    """The general form reduces the Courant step in the last stage's update;
+    a driver loop that stops at t_final, or an advance that is not taken,
+    keeps the step the last stage left: runs split anywhere give the same
+    clock and bits as one run."""
+    s, P = make()
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        dt = g.courant()
+    t_final = 7.5 * dt * s.cfl
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        n = g.run(100, s.cfl, t_final)
+        a = g.download()
+        t_a = g.t
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        n1 = g.run(3, s.cfl, t_final)
+        n2 = g.run(100, s.cfl, t_final)
+        n3 = g.run(100, s.cfl, t_final)
+        b = g.download()
+        t_b = g.t
+    assert n1 == 3 and n1 + n2 == n and n3 == 0
+    assert t_a == t_b
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
