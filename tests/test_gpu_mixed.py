@@ -28,6 +28,22 @@ def _cases():
     out.append(("kh96-fused-pcm-rk1-reflect", sr, W.apply_bc_numpy(sr, P.copy()), 10))
     so = s.with_(bc="outflow")
     out.append(("kh96-fused-plm-outflow", so, W.apply_bc_numpy(so, P.copy()), 10))
+    # hydro on the general form: WENO5 (the fused tiles take PCM / PLM only)
+    # with HLLC, and a 3-D blast (the fused tiles are 1-D / 2-D), so the
+    # face fluxes run on every compile-time axis
+    sw = s.with_(recon="weno5")
+    Pw = W.empty_state(sw)
+    g, gw, n = s.ng[0], sw.ng[0], s.shape[0]
+    Pw[gw:gw + n, gw:gw + n] = P[g:g + n, g:g + n]
+    out.append(("kh96-general-weno5-hllc", sw, W.apply_bc_numpy(sw, Pw), 8))
+    sb = W.Scheme(law="hydro", recon="plm", riemann="hllc", bc="periodic", rk_order=2, shape=(24, 24, 24),
+                  gamma=1.4, plm_theta=1.5, cfl=0.4, t_final=None, steps=8)
+    Pb = W.empty_state(sb)
+    X, Y, Z = W.cell_centres(sb)
+    r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2)
+    Pb[..., 0] = 1.0
+    Pb[..., 4] = np.where(r < 0.2, 10.0, 0.1)
+    out.append(("blast24cube-general-plm-hllc", sb, W.apply_bc_numpy(sb, Pb), 8))
     s, P = W.mhd_turbulence(16, rk_order=3)
     out.append(("mhd16cube-general-ct", s, P, 6))
     s, P = W.rmhd_blast(48)
