@@ -1,0 +1,82 @@
+"""Parity at the benchmarked sizes.
+
+The plain FP64 path against the oracle on the Kelvin-Helmholtz workload at
+1024^2 (the headline configuration), bit for bit over a few steps, and the
+mixed path against the oracle on the relativistic blast at 512^2; then
+size-independent properties of the mixed path at the benchmark sizes: on a
+periodic grid every face flux enters two zones with opposite signs, so the
+volume totals of mass, momentum and energy (and, with flux CT, of the
+magnetic flux) stay at their initial values to round-off, and flux CT keeps
+div B at round-off on MHD 256^3."""
+import numpy as np
+import pytest
+
+from helpers import oracle_config, rel_l1_max
+from mara2_gb300 import workloads as W
+from mara2_gb300.solver import Solver
+
+
+@pytest.mark.gpu
+def test_kh1024_plain_matches_oracle_bitwise(gpu_lib, port):
+    s, P = W.kelvin_helmholtz(1024)
+    ref = P.copy()
+    status, _, dts = port.run(oracle_config(s), ref, 3, s.cfl, s.t_final)
+    assert status == 0 and len(dts) == 3
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        for dt in dts:
+            g.advance(dt)
+        out = g.download()
+    assert np.array_equal(out[s.interior()].view(np.uint64), ref[s.interior()].view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_rmhd512_mixed_close_to_oracle(gpu_lib, port):
+    s, P = W.rmhd_blast(512)
+    ref = P.copy()
+    status, _, dts = port.run(oracle_config(s), ref, 2, s.cfl, s.t_final)
+    assert status == 0
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        for dt in dts:
+            g.advance(dt)
+        out = g.download()
+        assert g.stats().failures == 0
+    err = rel_l1_max(out[s.interior()], ref[s.interior()])
+    assert err[0] <= 1e-5, err.tolist()
+
+
+def _drift(d0, d1, names, scale):
+    return {k: abs(d1[k] - d0[k]) / scale for k in names}
+
+
+@pytest.mark.gpu
+def test_kh1024_mixed_conserves_totals(gpu_lib):
+    s, P = W.kelvin_helmholtz(1024)
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        d0 = g.volume_diagnostics()
+        assert g.run(50) == 50
+        d1 = g.volume_diagnostics()
+    # momentum and energy measured against the total mass (the momentum
+    # totals are near zero; the velocities and the energy per mass are O(1))
+    drift = _drift(d0, d1, ["mass", "momentum1", "momentum2", "total_energy"], d0["mass"])
+    assert max(drift.values()) < 1e-9, drift
+
+
+@pytest.mark.gpu
+def test_mhd256_mixed_conserves_totals_and_div_b(gpu_lib):
+    s, P = W.mhd_turbulence(256)
+    dx = 1.0 / 256
+    bmax = float(np.abs(P[..., 5:8]).max())
+    with Solver(s, "mixed") as g:
+        g.upload(P.copy())
+        d0 = g.volume_diagnostics()
+        assert g.run(3) == 3
+        d1 = g.volume_diagnostics()
+        m1 = g.monopole_max(dx)
+    names = ["mass", "momentum1", "momentum2", "momentum3", "total_energy",
+             "magnetic_flux1", "magnetic_flux2", "magnetic_flux3"]
+    drift = _drift(d0, d1, names, d0["mass"])
+    assert max(drift.values()) < 1e-9, drift
+    assert m1 * dx / bmax < 1e-5, m1 * dx / bmax
