@@ -48,7 +48,7 @@ template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 
 // normal); AXIS < 0 takes it, and the normal, at run time.
 template <int LAW, int RECON, int RIEMANN, int AXIS>
 __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P, float* __restrict__ F, GridF G,
-                                                     int axis, int lo0, int lo1, int lo2, int nb0,
+                                                     int axis, int lo0, int lo1, int lo2, int nb0, int nb1,
                                                      const int* __restrict__ done, DevStatus* st)
 {
     if constexpr (AXIS >= 0) axis = AXIS;
@@ -56,9 +56,12 @@ __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P
     constexpr int S = SOf<RECON>::S;
     if (*done || st->code) return;
     if (st->failures) { st->halt = 1; return; }
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nb0) return;
-    const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
+    // the faces of one z-slice as one index space (rows of n + 1 or n + 2
+    // faces would leave a nearly empty block per row)
+    const unsigned lin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lin >= (unsigned) nb0 * (unsigned) nb1) return;
+    const int t = (int) (lin % (unsigned) nb0);
+    const int i = lo0 + t, j = lo1 + (int) (lin / (unsigned) nb0), k = lo2 + blockIdx.y;
     const long long stride = axis == 0 ? 1 : axis == 1 ? (long long) G.N[0] : (long long) G.N[0] * G.N[1];
     const long long base = ((long long) k * G.N[1] + j) * G.N[0] + i;
     float PL[NQ], PR[NQ];
@@ -115,8 +118,9 @@ struct FluxViewF {
 __global__ void __launch_bounds__(128) ct_emf_kernel(FluxViewF V, float* E01, float* E02, float* E12, int M0, int M1,
                                                      int M2, int fx, int fy, int fz)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-    if (i >= M0) return;
+    const unsigned L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= (unsigned) M0 * (unsigned) M1) return;
+    const int i = (int) (L % (unsigned) M0), j = (int) (L / (unsigned) M0), k = blockIdx.y;
     const long long e = ((long long) k * M1 + j) * M0 + i;
     constexpr int B0 = 5, B1 = 6, B2 = 7;
     if (fx && fy && i > 0 && j > 0)
@@ -977,8 +981,8 @@ static void flux_f_launch(MixedState* m, int axis, const int* done, DevStatus* s
         else if (G.n[a] > 1) { const int e = G.ct ? 1 : 0; lo[a] = G.g[a] - e; nb[a] = G.n[a] + 2 * e; }
         else { lo[a] = 0; nb[a] = 1; }
     }
-    dim3 grid((nb[0] + 127) / 128, nb[1], nb[2]);
-#define MARA_FLUX_ARGS m->Pf, m->F[axis], G, axis, lo[0], lo[1], lo[2], nb[0], done, st
+    dim3 grid((unsigned) (((long long) nb[0] * nb[1] + 127) / 128), nb[2]);
+#define MARA_FLUX_ARGS m->Pf, m->F[axis], G, axis, lo[0], lo[1], lo[2], nb[0], nb[1], done, st
     // hydro and MHD fluxes take the axis at compile time; the relativistic
     // law's cost is its quartic, so it keeps one kernel for all axes
     if constexpr (LAW == LAW_RMHD) {
@@ -1035,7 +1039,7 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
             });
         }
         if (m->E[0]) {
-            dim3 eg((V.M0 + 127) / 128, V.M1, m->G.N[2] + 1);
+            dim3 eg((unsigned) (((long long) V.M0 * V.M1 + 127) / 128), m->G.N[2] + 1);
             timed(m, s, [&] {
                 ct_emf_kernel<<<eg, 128, 0, s>>>(V, m->E[0], m->E[1], m->E[2], V.M0, V.M1, m->G.N[2] + 1,
                                                  m->G.n[0] > 1, m->G.n[1] > 1, m->G.n[2] > 1);

@@ -43,16 +43,18 @@ __device__ __forceinline__ void record_status(DevStatus* st, int code)
 template <int LAW, int RECON, int RIEMANN>
 __global__ void __launch_bounds__(128) flux_kernel(const double* __restrict__ P, double* __restrict__ F,
                                                    GridDesc G, PhysParams pp, int axis,
-                                                   int lo0, int lo1, int lo2, int nb0,
+                                                   int lo0, int lo1, int lo2, int nb0, int nb1,
                                                    DevStatus* __restrict__ st)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
     constexpr int S = ReconInfo<RECON>::S;
     if (st->code != 0 || st->done) return;
     if (st->failures != 0) { st->halt = 1; return; }  // failures are final once the stage ended
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nb0) return;
-    const int i = lo0 + t, j = lo1 + blockIdx.y, k = lo2 + blockIdx.z;
+    // the faces of one z-slice as one index space (rows of n + 1 or n + 2
+    // faces would leave a nearly empty block per row)
+    const unsigned lin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lin >= (unsigned) nb0 * (unsigned) nb1) return;
+    const int i = lo0 + (int) (lin % (unsigned) nb0), j = lo1 + (int) (lin / (unsigned) nb0), k = lo2 + blockIdx.y;
     const long long stride = axis == 0 ? 1 : axis == 1 ? (long long) G.N[0] : (long long) G.N[0] * G.N[1];
     const long long base = ((long long) k * G.N[1] + j) * G.N[0] + i; // cell on the right of the face
     const double n[3] = {G.nrm[axis][0], G.nrm[axis][1], G.nrm[axis][2]};
@@ -319,8 +321,8 @@ static void flux_launch(int axis, const GridDesc& G, const PhysParams& pp, const
         else if (G.n[a] > 1) { const int e = G.ct ? 1 : 0; lo[a] = G.g[a] - e; nb[a] = G.n[a] + 2 * e; }
         else { lo[a] = 0; nb[a] = 1; }
     }
-    dim3 block(128), grid((nb[0] + 127) / 128, nb[1], nb[2]);
-    flux_kernel<LAW, RECON, RIEMANN><<<grid, block, 0, s>>>(P, F, G, pp, axis, lo[0], lo[1], lo[2], nb[0], st);
+    dim3 block(128), grid((unsigned) (((long long) nb[0] * nb[1] + 127) / 128), nb[2]);
+    flux_kernel<LAW, RECON, RIEMANN><<<grid, block, 0, s>>>(P, F, G, pp, axis, lo[0], lo[1], lo[2], nb[0], nb[1], st);
 }
 
 template <int LAW, int RECON>
