@@ -340,8 +340,10 @@ __device__ __forceinline__ int quartic_roots_f(float d4, float d3, float d2, flo
     } else if (delta < 0.f) {
         const float th = acosf(fminf(fmaxf(r / sqrtf(-q * q * q), -1.f), 1.f)) / 3.f;
         const float sq = sqrtf(-q);
-        const float x1 = 2.f * sq * cosf(th) - c2 / 3.f;
-        const float x3 = -sq * cosf(th) - c2 / 3.f + 1.7320508f * sq * sinf(th);
+        float sn, cs;
+        sincosf(th, &sn, &cs);
+        const float x1 = 2.f * sq * cs - c2 / 3.f;
+        const float x3 = -sq * cs - c2 / 3.f + 1.7320508f * sq * sn;
         u1 = fmaxf(x1, x3);
     } else {
         u1 = 2.f * cbrtf(r) - c2 / 3.f;
