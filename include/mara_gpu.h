@@ -287,12 +287,24 @@ int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
  * device image (held on every GPU that loads the library until the process
  * exits); grids whose intermediates exceed it return MARA_ERR_TOO_LARGE.
  * Calls share that array, so calls whose GPU work overlaps race: order them
- * on one stream.  The first call on a device looks the array up with the
- * device current; make it before any stream capture.  Synchronises the
- * stream and returns the step's status.  No counterpart in the reference:
+ * on one stream.  Each call looks the array's address up with
+ * config->device current (a host-side query, no allocation) and restores
+ * the caller's current device before it returns; the first call on a
+ * device may load the library's device image there, so make it before any
+ * stream capture.  Synchronises the stream and returns the step's status
+ * (MARA_ERR_CUDA only for this call's own launches and copies).  No counterpart in the reference:
  * it exists for callers of this library that cannot allocate. */
 int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const double* P_in, double* P_out,
                              double dt, void* stream);
+
+/* QuarticPolynomial::solve (src/QuarticPolynomial.cpp:19-144) on the device
+ * for n quartics d4 x^4 + d3 x^3 + d2 x^2 + d1 x + d0: coeffs (host) holds
+ * (d4, d3, d2, d1, d0) per quartic; roots (host) receives 4 values per
+ * quartic, the real roots in ascending order first (the rest 0), nroots
+ * (host) their number (0, 2 or 4).  The same device function as the RMHD
+ * eigenvalues of the plain path (its pow(x, 1/3), acos, cos and sin
+ * correctly rounded).  Synchronous; the caller's current device is kept. */
+int mara_gpu_quartic_solve(const double* coeffs, int n, double* roots, int* nroots, int device);
 
 const char* mara_gpu_status_string(int status);
 

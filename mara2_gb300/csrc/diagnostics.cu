@@ -106,3 +106,49 @@ void launch_volume_diag_plain(int law, const double* P, const GridDesc& G, const
 }
 
 } // namespace mara
+
+// ---- QuarticPolynomial::solve on the device ------------------------------------
+namespace mara {
+
+__global__ void k_quartic(const double* __restrict__ coeffs, int n, double* __restrict__ roots, int* __restrict__ nr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* d = coeffs + 5 * (long long) i;
+    double r[4] = {0.0, 0.0, 0.0, 0.0};
+    nr[i] = quartic_roots(d[0], d[1], d[2], d[3], d[4], r);
+    for (int k = 0; k < 4; ++k) roots[4 * (long long) i + k] = r[k];
+}
+
+} // namespace mara
+
+extern "C" int mara_gpu_quartic_solve(const double* coeffs, int n, double* roots, int* nroots, int device)
+{
+    using namespace mara;
+    if (n < 0 || (n > 0 && (!coeffs || !roots || !nroots))) return MARA_ERR_ARGUMENT;
+    if (n == 0) return MARA_OK;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    int rc = MARA_OK;
+    double* dc = nullptr;
+    double* dr = nullptr;
+    int* dn = nullptr;
+    const size_t cb = sizeof(double) * 5 * (size_t) n, rb = sizeof(double) * 4 * (size_t) n;
+    if (cudaMalloc(&dc, cb) != cudaSuccess || cudaMalloc(&dr, rb) != cudaSuccess ||
+        cudaMalloc(&dn, sizeof(int) * (size_t) n) != cudaSuccess) {
+        rc = MARA_ERR_CUDA;
+    } else if (cudaMemcpy(dc, coeffs, cb, cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = MARA_ERR_CUDA;
+    } else {
+        k_quartic<<<(n + 127) / 128, 128>>>(dc, n, dr, dn);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(roots, dr, rb, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(nroots, dn, sizeof(int) * (size_t) n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = MARA_ERR_CUDA;
+    }
+    cudaFree(dc);
+    cudaFree(dr);
+    cudaFree(dn);
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}

@@ -20,19 +20,20 @@
 //     fully overwritten before it is read;
 //   * calls whose GPU work overlaps (on different streams, or from different
 //     threads) race on the array: order them on one stream;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//   * every call looks up the array's device address (cudaGetSymbolAddress,
+//     host-side, allocates nothing) with config->device current, so a
+//     context that was torn down and created again is followed; the first
+//     call on a device may load the library's device image there, so make
+//     it before any stream capture;
+//   * the caller's current device is restored before the call returns.
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 
 #include "../../include/mara_gpu.h"
 #include "internal.h"
 
 #define MARA_NOALLOC_SCRATCH_BYTES (64ull << 20)
-#define MARA_NOALLOC_MAX_DEVICES 64
 
 // The scratch array.  In host code its name is only a host-side stand-in:
 // kernels must be given the device address looked up below.
@@ -45,9 +46,6 @@ namespace mara {
 int noalloc_validate(const MaraGpuConfig* c);
 void noalloc_make_grid(const MaraGpuConfig* c, GridDesc* G);
 
-static std::mutex g_lock;
-static unsigned char* g_scratch[MARA_NOALLOC_MAX_DEVICES] = {nullptr};
-
 __global__ void k_noalloc_begin(DevStatus* st, double dt)
 {
     DevStatus z;
@@ -59,44 +57,16 @@ __global__ void k_noalloc_begin(DevStatus* st, double dt)
 
 static size_t round_up(size_t n) { return (n + 255) & ~size_t(255); }
 
-} // namespace mara
-
-using namespace mara;
-
-extern "C" int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const double* P_in, double* P_out,
-                                        double dt, void* stream)
+// the advance proper, with config->device current
+static int noalloc_advance(const MaraGpuConfig* config, const GridDesc& G, size_t pbytes, size_t ubytes,
+                           size_t fbytes, const double* P_in, double* P_out, double dt, cudaStream_t s)
 {
-    if (!config || !P_in || !P_out) return MARA_ERR_ARGUMENT;
-    const int v = noalloc_validate(config);
-    if (v) return v;
-    if (config->precision != MARA_PRECISION_FP64) return MARA_ERR_CONFIG;
-    if (config->device < 0 || config->device >= MARA_NOALLOC_MAX_DEVICES) return MARA_ERR_NO_DEVICE;
-
-    GridDesc G;
-    noalloc_make_grid(config, &G);
-    const size_t pbytes = round_up(sizeof(double) * (size_t) G.sP * G.nq);
-    const size_t ubytes = round_up(sizeof(double) * (size_t) G.sU * G.nq);
-    const size_t fbytes = round_up(sizeof(double) * (size_t) G.sF * G.nq);
-    int axes = 0;
-    for (int a = 0; a < 3; ++a) axes += G.n[a] > 1;
-    const size_t need = round_up(sizeof(DevStatus)) + 2 * pbytes + 2 * ubytes + axes * fbytes;
-    if (need > MARA_NOALLOC_SCRATCH_BYTES) return MARA_ERR_TOO_LARGE;
-
-    if (cudaSetDevice(config->device) != cudaSuccess) return MARA_ERR_NO_DEVICE;
-    unsigned char* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_lock);
-        if (!g_scratch[config->device]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, mara_noalloc_scratch) != cudaSuccess || !p) return MARA_ERR_CUDA;
-            g_scratch[config->device] = (unsigned char*) p;
-        }
-        base = g_scratch[config->device];
-    }
-    cudaStream_t s = (cudaStream_t) stream;
+    // the scratch array's device address in the current context
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, mara_noalloc_scratch) != cudaSuccess || !p) return MARA_ERR_CUDA;
+    unsigned char* cur = (unsigned char*) p;
 
     // carve the scratch array
-    unsigned char* cur = base;
     DevStatus* st = (DevStatus*) cur;
     cur += round_up(sizeof(DevStatus));
     double* P[2];
@@ -129,12 +99,43 @@ extern "C" int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const doubl
         c = 1 - c;
     }
     launch_soa_to_aos(P[c], P_out, G, s);
+    // launch errors of this call only: checked before anything else runs
+    if (cudaGetLastError() != cudaSuccess) return MARA_ERR_CUDA;
 
     DevStatus host;
     if (cudaMemcpyAsync(&host, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MARA_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return MARA_ERR_CUDA;
-    if (cudaGetLastError() != cudaSuccess) return MARA_ERR_CUDA;
     if (host.code) return host.code;
     if (host.failures > 0) return MARA_ERR_INVERSION_FAILURE;
     return MARA_OK;
+}
+
+} // namespace mara
+
+using namespace mara;
+
+extern "C" int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const double* P_in, double* P_out,
+                                        double dt, void* stream)
+{
+    if (!config || !P_in || !P_out) return MARA_ERR_ARGUMENT;
+    const int v = noalloc_validate(config);
+    if (v) return v;
+    if (config->precision != MARA_PRECISION_FP64) return MARA_ERR_CONFIG;
+
+    GridDesc G;
+    noalloc_make_grid(config, &G);
+    const size_t pbytes = round_up(sizeof(double) * (size_t) G.sP * G.nq);
+    const size_t ubytes = round_up(sizeof(double) * (size_t) G.sU * G.nq);
+    const size_t fbytes = round_up(sizeof(double) * (size_t) G.sF * G.nq);
+    int axes = 0;
+    for (int a = 0; a < 3; ++a) axes += G.n[a] > 1;
+    const size_t need = round_up(sizeof(DevStatus)) + 2 * pbytes + 2 * ubytes + axes * fbytes;
+    if (need > MARA_NOALLOC_SCRATCH_BYTES) return MARA_ERR_TOO_LARGE;
+
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    if (prev != config->device && cudaSetDevice(config->device) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    const int rc = noalloc_advance(config, G, pbytes, ubytes, fbytes, P_in, P_out, dt, (cudaStream_t) stream);
+    if (prev != config->device) cudaSetDevice(prev);
+    return rc;
 }

@@ -5,12 +5,16 @@
 // this header are compiled with --fmad=false, so the plain path rounds
 // exactly as the reference's CPU build (-ffp-contract=off) does.  Divisions
 // and square roots are IEEE round-to-nearest in CUDA FP64.  The quartic's
-// pow/acos/cos/sin are CUDA's own (within 2 ulp), the one place where the
-// plain path may differ from the reference by a rounding.
+// pow(x, 1/3), acos, cos and sin are the correctly rounded evaluations of
+// crmath.cuh; the reference's libm (glibc) returns the correctly rounded
+// value on all but ~0.1 % of arguments, the one place where the plain path
+// may differ from the reference by a rounding.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "crmath.cuh"
 
 namespace mara {
 
@@ -257,15 +261,15 @@ __device__ __forceinline__ void solve_cubic(double c3, double c2, double c1, dou
     if (delta > 0.0) {
         double s1 = r + sqrt(delta);
         double s2 = r - sqrt(delta);
-        s1 = (s1 >= 0.0) ? pow(s1, 1. / 3) : -pow(-s1, 1. / 3);
-        s2 = (s2 >= 0.0) ? pow(s2, 1. / 3) : -pow(-s2, 1. / 3);
+        s1 = (s1 >= 0.0) ? crm::pow_third(s1) : -crm::pow_third(-s1);
+        s2 = (s2 >= 0.0) ? crm::pow_third(s2) : -crm::pow_third(-s2);
         x1 = (s1 + s2) - a2 / 3.0;
         x2 = x3 = -0.5 * (s1 + s2) - a2 / 3.0;
         nr = 1;
     } else if (delta < 0.0) {
-        const double theta = acos(r / sqrt(-q * q * q)) / 3.0;
-        const double costh = cos(theta);
-        const double sinth = sin(theta);
+        const double theta = crm::acos_cr(r / sqrt(-q * q * q)) / 3.0;
+        const double costh = crm::cos_cr(theta);
+        const double sinth = crm::sin_cr(theta);
         const double sq = sqrt(-q);
         const double rt3 = 1.7320508075688772; // sqrt(3), correctly rounded
         x1 = 2.0 * sq * costh - a2 / 3.0;
@@ -273,7 +277,7 @@ __device__ __forceinline__ void solve_cubic(double c3, double c2, double c1, dou
         x3 = -sq * costh - a2 / 3.0 + rt3 * sq * sinth;
         nr = 3;
     } else {
-        const double s = (r >= 0.0) ? pow(r, 1. / 3) : -pow(-r, 1. / 3);
+        const double s = (r >= 0.0) ? crm::pow_third(r) : -crm::pow_third(-r);
         x1 = 2.0 * s - a2 / 3.0;
         x2 = x3 = -s - a2 / 3.0;
         nr = 3;

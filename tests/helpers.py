@@ -31,19 +31,30 @@ def interior(s, P):
     return P[s.interior()]
 
 
-def rel_l1_max(a, b):
-    """L1 difference per conserved field relative to the largest field's L1
-    norm: used where CUDA's and glibc's transcendental functions (the RMHD
-    quartic's pow/acos/cos/sin) may differ in the last bit, which fields
-    that start at zero would otherwise magnify."""
+def parity_error(s, a, b):
+    """The parity metric of the plain path: relative L1 difference per
+    conserved field, for every law."""
+    return rel_l1(a, b)
+
+
+def rel_linf(a, b):
+    """L-infinity difference per conserved field relative to the field's
+    largest magnitude."""
     a = np.asarray(a, float)
     b = np.asarray(b, float)
-    nq = a.shape[-1]
-    big = max(np.sum(np.abs(b[..., q])) for q in range(nq))
-    return np.array([np.sum(np.abs(a[..., q] - b[..., q])) / big for q in range(nq)])
+    out = []
+    for q in range(a.shape[-1]):
+        den = np.max(np.abs(b[..., q]))
+        num = np.max(np.abs(a[..., q] - b[..., q]))
+        out.append(num / den if den > 0 else num)
+    return np.array(out)
 
 
-def parity_error(s, a, b):
-    """The parity metric of the plain path: relative L1 per conserved field,
-    or relative to the largest field for RMHD (see rel_l1_max)."""
-    return rel_l1_max(a, b) if s.law == "rmhd" else rel_l1(a, b)
+def rel_l1_max(a, b):
+    """L1 difference per conserved field relative to the largest field's L1
+    norm: the mixed path's measure for fields that start at exactly zero
+    (a transverse field or momentum), which have no norm of their own."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    big = max(np.sum(np.abs(b[..., q])) for q in range(a.shape[-1]))
+    return np.array([np.sum(np.abs(a[..., q] - b[..., q])) / big for q in range(a.shape[-1])])

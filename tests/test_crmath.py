@@ -1,0 +1,135 @@
+"""The correctly rounded pow(x, 1/3), acos, cos and sin of the plain path's
+RMHD quartic (mara2_gb300/csrc/crmath.cuh).
+
+* On the CPU: the header compiled for the host returns the correctly rounded
+  value (checked against 60-digit decimal arithmetic) on seeded arguments
+  over the ranges the resolvent cubic passes, and the host's libm is
+  reported beside it.
+* On the GPU: the device evaluation gives the same bits as the host one on
+  a million arguments per function, and differs from the host's libm (the
+  reference's arithmetic) on far fewer arguments than CUDA's own functions;
+  the counts are printed as the ulp table of the quartic's functions.
+"""
+import ctypes as C
+import math
+import os
+import shutil
+import subprocess
+from decimal import Decimal as D, getcontext
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PROBE = os.path.join(ROOT, "tests", "crmath_probe.cu")
+NAMES = ("pow(x,1/3)", "acos", "cos", "sin")
+Y3 = float.fromhex("0x1.5555555555555p-2")   # fl(1/3), the exponent the reference passes
+
+
+def arguments(fn, n, seed=2026):
+    rng = np.random.default_rng(seed + fn)
+    if fn == 0:
+        x = np.where(rng.random(n) < 0.5, 10.0 ** rng.uniform(-30, 30, n), rng.uniform(0, 10, n))
+    elif fn == 1:
+        u = rng.random(n)
+        x = rng.uniform(-1, 1, n)
+        x = np.where(u < 0.2, 1 - 10.0 ** rng.uniform(-16, -1, n), x)
+        x = np.where(u > 0.8, -1 + 10.0 ** rng.uniform(-16, -1, n), x)
+    else:
+        x = np.where(rng.random(n) < 0.2, 10.0 ** rng.uniform(-20, 0, n) * 1.0471975511965976,
+                     rng.uniform(0, 1.0471975511965976, n))
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _build_host(tmp):
+    so = os.path.join(tmp, "libcrprobe_host.so")
+    subprocess.run(["g++", "-x", "c++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", PROBE,
+                    "-o", so, "-lm"], check=True)
+    return C.CDLL(so)
+
+
+def _eval(lib, name, fn, x, outs=2):
+    n = len(x)
+    ys = [np.empty(n) for _ in range(outs)]
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    rc = getattr(lib, name)(C.c_int(fn), ptr(x), C.c_int(n), *[ptr(y) for y in ys])
+    assert rc in (None, 0)
+    return ys
+
+
+# ---- 60-digit references ----------------------------------------------------------
+getcontext().prec = 60
+
+
+def _sin(x):
+    s, t, n = D(0), x, 1
+    while abs(t) > D(10) ** -60:
+        s += t
+        n += 2
+        t = -t * x * x / ((n - 1) * n)
+    return s
+
+
+def _cos(x):
+    s, t, n = D(0), D(1), 0
+    while abs(t) > D(10) ** -60:
+        s += t
+        n += 2
+        t = -t * x * x / ((n - 1) * n)
+    return s
+
+
+def _acos(z):
+    t = D(math.acos(float(z)))
+    for _ in range(5):
+        t = t + (_cos(t) - z) / _sin(t)
+    return t
+
+
+def exact(fn, x):
+    X = D(float(x))
+    if fn == 0:
+        return float(X ** D(Y3)) if x > 0 else 0.0
+    return float((_acos, _cos, _sin)[fn - 1](X))
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+@pytest.mark.parametrize("fn", range(4), ids=NAMES)
+def test_host_evaluation_is_correctly_rounded(tmp_path, fn):
+    lib = _build_host(str(tmp_path))
+    x = arguments(fn, 3000)
+    libm, cr = _eval(lib, "host_eval", fn, x)
+    want = np.array([exact(fn, v) for v in x[:400]])
+    assert np.array_equal(_bits(cr[:400]), _bits(want)), NAMES[fn]
+    off = int(np.count_nonzero(_bits(libm) != _bits(cr)))
+    print(f"{NAMES[fn]}: host libm differs from the correctly rounded value on {off} of {len(x)}")
+
+
+@pytest.mark.gpu
+def test_device_evaluation_matches_host_and_libm(tmp_path):
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    so = os.path.join(str(tmp_path), "libcrprobe_dev.so")
+    subprocess.run([nvcc, "-O3", "-std=c++17", "--fmad=false", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared", PROBE, "-o", so], check=True)
+    lib = C.CDLL(so)
+    n = 1 << 20
+    rows = []
+    for fn in range(4):
+        x = arguments(fn, n, seed=77)
+        libm, cr_host = _eval(lib, "host_eval", fn, x)
+        cuda, cr_dev = _eval(lib, "dev_eval", fn, x)
+        assert np.array_equal(_bits(cr_dev), _bits(cr_host)), NAMES[fn]
+        ulp = lambda a, b: np.abs(_bits(a).astype(np.int64) - _bits(b).astype(np.int64))
+        u_cuda, u_cr = ulp(cuda, libm), ulp(cr_dev, libm)
+        rows.append((NAMES[fn], int(np.count_nonzero(u_cuda)), int(u_cuda.max()), int(np.count_nonzero(u_cr)),
+                     int(u_cr.max())))
+        assert np.count_nonzero(u_cr) < np.count_nonzero(u_cuda)
+        assert np.count_nonzero(u_cr) <= 0.005 * n
+        assert u_cr.max() <= 1
+    print(f"\nulp gaps to the host libm over {n} arguments per function:")
+    print("function      CUDA: differ / max ulp    crmath: differ / max ulp")
+    for r in rows:
+        print(f"{r[0]:<12}  {r[1]:>10} / {r[2]:<8}      {r[3]:>10} / {r[4]}")

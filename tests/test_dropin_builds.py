@@ -12,7 +12,7 @@ import pytest
 import oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.environ.get("MARA_REF_SRC", "/root/reference/src")
+REF_SRC = os.environ.get("MARA_REF_SRC", os.path.join(ROOT, "baseline", "_ref", "src"))
 
 DRIVER = r'''
 #include "GpuSolutionScheme.hpp"

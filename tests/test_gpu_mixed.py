@@ -8,7 +8,7 @@ a wide margin, for every law and both kernel families."""
 import numpy as np
 import pytest
 
-from helpers import oracle_config, rel_l1
+from helpers import oracle_config, rel_l1, rel_l1_max, rel_linf
 from mara2_gb300 import workloads as W
 from mara2_gb300.solver import Solver
 
@@ -76,8 +76,13 @@ def test_mixed_close_to_fp64_oracle(gpu_lib, port, name, s, P, steps):
             g.advance(dt)
         g.synchronize()
         out = g.download()
-    err = rel_l1(out[s.interior()], ref[s.interior()])
+    a, b = out[s.interior()], ref[s.interior()]
+    err = rel_l1(a, b)
+    print(name, "L1 per field:", err.tolist(), "Linf per field:", rel_linf(a, b).tolist())
     assert err[0] <= TOL_RHO, (name, err)
+    # every field, against the largest field's norm (fields that start at
+    # zero have no norm of their own to measure against)
+    assert np.all(rel_l1_max(a, b) <= TOL_RHO), (name, rel_l1_max(a, b))
     assert np.all(np.isfinite(out))
 
 
@@ -95,7 +100,7 @@ def test_mixed_driver_loop_runs_to_end_time(gpu_lib, port):
     assert abs(g.t - s.t_final) < 1e-12
     assert abs(n - len(dts)) <= 2          # FP32 Courant steps may differ slightly
     err = rel_l1(out[s.interior()], ref[s.interior()])
-    assert err[0] < 1e-4, err
+    assert err[0] <= TOL_RHO, err
 
 
 @pytest.mark.gpu
@@ -181,7 +186,7 @@ def test_cluster_run_stops_at_t_final_and_continues(gpu_lib, port):
         assert abs(g.t - s.t_final) < 1e-12
     assert n1 == 100 and abs((n1 + n2) - len(dts)) <= 2
     err = rel_l1(out[s.interior()], ref[s.interior()])
-    assert err[0] < 1e-4, err
+    assert err[0] <= TOL_RHO, err
 
 
 @pytest.mark.gpu

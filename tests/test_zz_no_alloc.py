@@ -3,20 +3,21 @@ device memory when they step a grid (an application whose memory pool
 already reserves the GPU, a latency-critical loop that must not block in an
 allocation, code that must avoid cudaFree's device-wide synchronisation).
 
-Checked through the C ABI against the handle-based entry points
-(mara_gpu_create / upload / advance / download), two calls in a row on the
-same device buffers, within the tolerance of the plain-path parity tests.
-This file is collected last so that a run stopping at the first failure has
-already run every other test; it passes alone in a fresh process too.
+The entry point runs the same plain FP64 kernels as the handle-based entry
+points (mara_gpu_create / upload / advance / download), so it is checked
+against them bit for bit, through the C ABI, two calls in a row on the same
+device buffers: a 2-D hydro Kelvin-Helmholtz grid (RK2, HLLC) and a 3-D MHD
+grid with constrained transport (RK3, HLLE, three face-flux arrays carved
+from the scratch array).  A planted state that cannot be inverted must come
+back as the same status code the handle path reports, and the caller's
+current device must be unchanged afterwards.  This file is collected last,
+so that a run stopping at the first failure has already run every other
+test; it passes alone in a fresh process too.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
-
-from helpers import rel_l1
-
-TOL = 1e-12  # relative L1 per conserved field, as in the plain-path parity tests
 
 
 def _noalloc(lib, cfg, d_in, d_out, dt, stream):
@@ -24,14 +25,15 @@ def _noalloc(lib, cfg, d_in, d_out, dt, stream):
                                         dt, C.c_void_p(stream))
 
 
-@pytest.mark.gpu
-def test_noalloc_matches_handle_path_two_calls(gpu_lib):
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def _two_steps_both_ways(lib, s, P0):
     import torch
     from mara2_gb300 import _native as N
-    from mara2_gb300 import workloads as W
     from mara2_gb300.solver import Solver
 
-    s, P0 = W.kelvin_helmholtz(64)
     cfg = N.config_from_scheme(s, "fp64", 0)
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
@@ -50,15 +52,63 @@ def test_noalloc_matches_handle_path_two_calls(gpu_lib):
     d_in = torch.from_numpy(P0.copy()).to(dev)
     d_out = torch.empty_like(d_in)
     torch.cuda.synchronize(dev)
-    assert _noalloc(gpu_lib, cfg, d_in, d_out, dt1, stream.cuda_stream) == N.MARA_OK
+    assert _noalloc(lib, cfg, d_in, d_out, dt1, stream.cuda_stream) == N.MARA_OK
     out1 = d_out.cpu().numpy()
-    assert _noalloc(gpu_lib, cfg, d_out, d_out, dt2, stream.cuda_stream) == N.MARA_OK  # in place
+    assert _noalloc(lib, cfg, d_out, d_out, dt2, stream.cuda_stream) == N.MARA_OK  # in place
     out2 = d_out.cpu().numpy()
+    assert torch.cuda.current_device() == 0
+    return (ref1, ref2), (out1, out2)
 
+
+@pytest.mark.gpu
+def test_noalloc_matches_handle_path_two_calls_hydro(gpu_lib):
+    from mara2_gb300 import workloads as W
+
+    s, P0 = W.kelvin_helmholtz(64)
+    (ref1, ref2), (out1, out2) = _two_steps_both_ways(gpu_lib, s, P0)
     i = s.interior()
-    assert np.all(rel_l1(out1[i], ref1[i]) <= TOL)
-    assert np.all(rel_l1(out2[i], ref2[i]) <= TOL)
+    assert np.array_equal(_bits(out1[i]), _bits(ref1[i]))
+    assert np.array_equal(_bits(out2[i]), _bits(ref2[i]))
     assert np.all(np.isfinite(out2))
+
+
+@pytest.mark.gpu
+def test_noalloc_matches_handle_path_two_calls_mhd3d_rk3(gpu_lib):
+    from mara2_gb300 import workloads as W
+
+    s, P0 = W.mhd_turbulence(12)
+    assert s.rk_order == 3 and s.law == "mhd" and s.dims == 3
+    (ref1, ref2), (out1, out2) = _two_steps_both_ways(gpu_lib, s, P0)
+    i = s.interior()
+    assert np.array_equal(_bits(out1[i]), _bits(ref1[i]))
+    assert np.array_equal(_bits(out2[i]), _bits(ref2[i]))
+
+
+@pytest.mark.gpu
+def test_noalloc_reports_inversion_failure_like_the_handle_path(gpu_lib):
+    import torch
+    from mara2_gb300 import _native as N
+    from mara2_gb300 import workloads as W
+    from mara2_gb300.solver import Solver
+
+    s, P = W.mhd_turbulence(6)
+    Q = P.copy()
+    Q[4, 5, 3, 4] = 1e-9     # near-vacuum pressure next to a strong velocity jump
+    Q[4, 5, 3, 1] = 3.0
+    with Solver(s, "fp64") as g:
+        g.upload(Q.copy())
+        g.advance(0.05)
+        want = g.status()
+    assert want == N.MARA_ERR_INVERSION_FAILURE
+    cfg = N.config_from_scheme(s, "fp64", 0)
+    d = torch.from_numpy(Q.copy()).to("cuda:0")
+    out = torch.empty_like(d)
+    torch.cuda.synchronize()
+    assert _noalloc(gpu_lib, cfg, d, out, 0.05, torch.cuda.current_stream().cuda_stream) == want
+    # the next call starts from cleared status words
+    s2, P2 = W.mhd_turbulence(6)
+    d2 = torch.from_numpy(P2.copy()).to("cuda:0")
+    assert _noalloc(gpu_lib, cfg, d2, out, 1e-3, torch.cuda.current_stream().cuda_stream) == N.MARA_OK
 
 
 @pytest.mark.gpu
