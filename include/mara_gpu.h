@@ -297,6 +297,38 @@ int64_t mara_gpu_device_bytes(const MaraGpuHandle* h);
 int mara_gpu_advance_noalloc(const MaraGpuConfig* config, const double* P_in, double* P_out,
                              double dt, void* stream);
 
+/* ---- the ConstrainedTransport interface (src/Mara.hpp:341-349) -------------
+ * Device forms of UniformCartesianCT (src/ConstrainedTransport.cpp), the
+ * reference's implementation of the interface: a cell-centred field B (host,
+ * AoS (n[0], n[1], n[2], 3)) as assignCellCenteredB receives it, given one
+ * guard zone on every axis by the boundary condition (MARA_BC_PERIODIC or
+ * MARA_BC_OUTFLOW; MARA_ERR_CONFIG otherwise).
+ *   mara_gpu_ct_monopole: computeMonopole (ConstrainedTransport.cpp:81-89,
+ *     302-377) at vertices (location 0; M (n+1)^3 values) or cells
+ *     (location 1; M n^3 values).
+ *   mara_gpu_ct_current: computeCurrent as CellCenteredFieldCT::current
+ *     (CellCenteredFieldCT.cpp:231-257) with the given mesh spacing at the
+ *     interior cells (J (n[0], n[1], n[2], 3)).  UniformCartesianCT's own
+ *     computeCurrent (ConstrainedTransport.cpp:91-117) reads components 1..3
+ *     of a 3-component array and offsets -1..+1 of a 0..2 stencil window, so
+ *     it has no defined result to follow.
+ * Synchronous; the caller's current device is kept. */
+int mara_gpu_ct_monopole(const double* B, const int n[3], int bc, int location, double* M, int device);
+int mara_gpu_ct_current(const double* B, const int n[3], int bc, double mesh_spacing, double* J, int device);
+
+/* The divergence-free initial field of the reference's MHD drivers
+ * (src/Problems.cpp:660-667) on the resident state: the face-centred vector
+ * potential A (host, MeshOperator::generate(ivp, face, scalars, guards):
+ * (N0+1, N1+1, N2+1, 3, 3) over the cells with guards, component then face
+ * axis) becomes Godunov fluxes (CellCenteredFieldCT::vectorPotentialToFluxes,
+ * CellCenteredFieldCT.cpp:136-150), flux CT (generateGodunovFluxes, :152-157)
+ * and their divergence (MeshOperator::divergence, factor 1), times scale;
+ * the result replaces the magnetic field of every interior cell
+ * (MeshData::assignMagneticField) and the guards are refilled by the boundary
+ * condition (applyBoundaryCondition).  MHD and RMHD handles, either
+ * precision; the arithmetic is FP64 and gives the reference's bits. */
+int mara_gpu_assign_vector_potential(MaraGpuHandle* h, const double* A, double scale);
+
 /* QuarticPolynomial::solve (src/QuarticPolynomial.cpp:19-144) on the device
  * for n quartics d4 x^4 + d3 x^3 + d2 x^2 + d1 x + d0: coeffs (host) holds
  * (d4, d3, d2, d1, d0) per quartic; roots (host) receives 4 values per

@@ -98,6 +98,9 @@ SIGNATURES = {
     "mara_gpu_field_diagnostics": (C.c_int, [_H, C.c_double, C.c_void_p]),
     "mara_gpu_status_string": (C.c_char_p, [C.c_int]),
     "mara_gpu_quartic_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "mara_gpu_ct_monopole": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]),
+    "mara_gpu_ct_current": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_int]),
+    "mara_gpu_assign_vector_potential": (C.c_int, [_H, C.c_void_p, C.c_double]),
     "mara_gpu_advance_noalloc": (C.c_int, [C.POINTER(MaraGpuConfig), C.c_void_p, C.c_void_p, C.c_double,
                                            C.c_void_p]),
 }

@@ -227,3 +227,74 @@ private:
     mutable MaraGpuHandle* handle = nullptr;
     mutable double* pinned = nullptr;   // the page-locked MeshData::P, if any
 };
+
+/** The ConstrainedTransport interface (src/Mara.hpp:341-349) on the GPU, as
+ *  its reference implementation UniformCartesianCT (src/ConstrainedTransport
+ *  .cpp) behaves for a cell-centred field: assignCellCenteredB stores the
+ *  interior field, the guards (one zone per axis) come from the boundary
+ *  condition (periodic or outflow), computeMonopole runs the vertex / cell
+ *  monopole on the device (mara_gpu_ct_monopole), computeCurrent the
+ *  centred-difference curl of CellCenteredFieldCT::current with unit mesh
+ *  spacing (mara_gpu_ct_current).  Errors are std::logic_error, as the
+ *  reference throws for a bad mesh location. */
+class GpuConstrainedTransport : public ConstrainedTransport
+{
+public:
+    explicit GpuConstrainedTransport (int device = 0) : device (device) {}
+
+    void setMeshGeometry (std::shared_ptr<MeshGeometry> geometry) override { meshGeometry = geometry; }
+    void setBoundaryCondition (std::shared_ptr<BoundaryCondition> bc) override
+    {
+        if      (dynamic_cast<const PeriodicBoundaryCondition*> (bc.get())) bcKind = MARA_BC_PERIODIC;
+        else if (dynamic_cast<const OutflowBoundaryCondition*>  (bc.get())) bcKind = MARA_BC_OUTFLOW;
+        else throw std::logic_error ("GpuConstrainedTransport: periodic or outflow boundaries only");
+    }
+
+    void assignCellCenteredB (Cow::Array newB) override
+    {
+        if (! meshGeometry) throw std::logic_error ("GpuConstrainedTransport: no mesh geometry");
+        const auto cells = meshGeometry->cellsShape();
+        if (newB.size (0) != cells[0] || newB.size (1) != cells[1] || newB.size (2) != cells[2] || newB.size (3) != 3)
+            throw std::logic_error ("GpuConstrainedTransport: field shape does not match the mesh");
+        B = std::move (newB);
+    }
+
+    Cow::Array computeMonopole (MeshLocation location) const override
+    {
+        int n[3];
+        shape (n);
+        if (location != MeshLocation::vert && location != MeshLocation::cell)
+            throw std::logic_error ("Mesh location for monopole calculation not cell or vert");
+        const int v = location == MeshLocation::vert ? 1 : 0;
+        auto M = Cow::Array (n[0] + v, n[1] + v, n[2] + v);
+        check (mara_gpu_ct_monopole (B.data(), n, bcKind, v ? 0 : 1, M.data(), device));
+        return M;
+    }
+
+    Cow::Array computeCurrent (MeshLocation location) const override
+    {
+        if (location != MeshLocation::cell)
+            throw std::logic_error ("Mesh location for current calculation not cell");
+        int n[3];
+        shape (n);
+        auto J = Cow::Array (n[0], n[1], n[2], 3);
+        check (mara_gpu_ct_current (B.data(), n, bcKind, 1.0, J.data(), device));
+        return J;
+    }
+
+private:
+    void shape (int n[3]) const
+    {
+        if (B.size() == 0) throw std::logic_error ("GpuConstrainedTransport: no field assigned");
+        for (int a = 0; a < 3; ++a) n[a] = B.size (a);
+    }
+    static void check (int status)
+    {
+        if (status != MARA_OK)
+            throw std::logic_error (std::string ("GpuConstrainedTransport: ") + mara_gpu_status_string (status));
+    }
+    int device = 0;
+    int bcKind = MARA_BC_PERIODIC;
+    std::shared_ptr<MeshGeometry> meshGeometry;
+    Cow::Array B;
+};

@@ -152,3 +152,125 @@ extern "C" int mara_gpu_quartic_solve(const double* coeffs, int n, double* roots
     if (prev != device) cudaSetDevice(prev);
     return rc;
 }
+
+// ---- the ConstrainedTransport interface (src/Mara.hpp:341-349) -------------------
+// UniformCartesianCT (src/ConstrainedTransport.cpp) keeps a cell-centred field
+// with one guard zone on every axis, filled by the boundary condition axis by
+// axis (setCellBC); here a guard index is read from its interior image.
+namespace mara {
+
+struct UctField {
+    const double* B;   // interior cells (n0, n1, n2, 3), AoS, C order
+    int n0, n1, n2, bc;
+    // guarded index I in [0, n + 1] -> interior index
+    __device__ __forceinline__ static int img(int I, int n, int bc)
+    {
+        if (I >= 1 && I <= n) return I - 1;
+        if (bc == BC_PERIODIC) return I == 0 ? n - 1 : 0;
+        return I == 0 ? 0 : n - 1;
+    }
+    __device__ __forceinline__ double operator()(int I, int J, int K, int q) const
+    {
+        const int i = img(I, n0, bc), j = img(J, n1, bc), k = img(K, n2, bc);
+        return B[(((long long) i * n1 + j) * n2 + k) * 3 + q];
+    }
+};
+
+// computeMonopoleVert (ConstrainedTransport.cpp:302-356) at vertex (i, j, k)
+__device__ __forceinline__ double uct_vertex_monopole(const UctField& B, int i, int j, int k)
+{
+    const double Bx0 = B(i + 0, j + 0, k + 0, 0) + B(i + 0, j + 0, k + 1, 0) + B(i + 0, j + 1, k + 0, 0) + B(i + 0, j + 1, k + 1, 0);
+    const double Bx1 = B(i + 1, j + 0, k + 0, 0) + B(i + 1, j + 0, k + 1, 0) + B(i + 1, j + 1, k + 0, 0) + B(i + 1, j + 1, k + 1, 0);
+    const double By0 = B(i + 0, j + 0, k + 0, 1) + B(i + 1, j + 0, k + 0, 1) + B(i + 0, j + 0, k + 1, 1) + B(i + 1, j + 0, k + 1, 1);
+    const double By1 = B(i + 0, j + 1, k + 0, 1) + B(i + 1, j + 1, k + 0, 1) + B(i + 0, j + 1, k + 1, 1) + B(i + 1, j + 1, k + 1, 1);
+    const double Bz0 = B(i + 0, j + 0, k + 0, 2) + B(i + 0, j + 1, k + 0, 2) + B(i + 1, j + 0, k + 0, 2) + B(i + 1, j + 1, k + 0, 2);
+    const double Bz1 = B(i + 0, j + 0, k + 1, 2) + B(i + 0, j + 1, k + 1, 2) + B(i + 1, j + 0, k + 1, 2) + B(i + 1, j + 1, k + 1, 2);
+    return 0.25 * ((Bx1 - Bx0) + (By1 - By0) + (Bz1 - Bz0));
+}
+
+// location 0: vertices (n0+1, n1+1, n2+1); 1: cells (computeMonopoleCell,
+// ConstrainedTransport.cpp:358-377)
+__global__ void k_uct_monopole(UctField B, int location, double* __restrict__ M)
+{
+    const int m0 = location == 0 ? B.n0 + 1 : B.n0, m1 = location == 0 ? B.n1 + 1 : B.n1;
+    const int m2 = location == 0 ? B.n2 + 1 : B.n2;
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= (long long) m0 * m1 * m2) return;
+    const int k = (int) (c % m2), j = (int) ((c / m2) % m1), i = (int) (c / ((long long) m2 * m1));
+    if (location == 0) {
+        M[c] = uct_vertex_monopole(B, i, j, k);
+        return;
+    }
+    const double M000 = uct_vertex_monopole(B, i, j, k);
+    const double Mi = 0.5 * (M000 + uct_vertex_monopole(B, i + 1, j, k));
+    const double Mj = 0.5 * (M000 + uct_vertex_monopole(B, i, j + 1, k));
+    const double Mk = 0.5 * (M000 + uct_vertex_monopole(B, i, j, k + 1));
+    M[c] = 1. / 3 * (Mi + Mj + Mk);
+}
+
+// CellCenteredFieldCT::current (CellCenteredFieldCT.cpp:231-257) of the
+// guarded field at interior cell (i, j, k): the reference's loop index is
+// the cell's guarded index minus one on every axis
+__global__ void k_uct_current(UctField B, double h, double* __restrict__ J)
+{
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (c >= (long long) B.n0 * B.n1 * B.n2) return;
+    const int k = (int) (c % B.n2), j = (int) ((c / B.n2) % B.n1), i = (int) (c / ((long long) B.n2 * B.n1));
+    const double d0B1 = B(i + 2, j, k, 1) - B(i, j, k, 1);
+    const double d0B2 = B(i + 2, j, k, 2) - B(i, j, k, 2);
+    const double d1B2 = B(i, j + 2, k, 2) - B(i, j, k, 2);
+    const double d1B0 = B(i, j + 2, k, 0) - B(i, j, k, 0);
+    const double d2B0 = B(i, j, k + 2, 0) - B(i, j, k, 0);
+    const double d2B1 = B(i, j, k + 2, 1) - B(i, j, k, 1);
+    J[c * 3 + 0] = (d1B2 - d2B1) / h / 2;
+    J[c * 3 + 1] = (d2B0 - d0B2) / h / 2;
+    J[c * 3 + 2] = (d0B1 - d1B0) / h / 2;
+}
+
+// host arrays in and out; which = 0 monopole, 1 current
+static int uct_call(const double* B, const int n[3], int bc, int which, int location, double h, double* out,
+                    int device)
+{
+    if (!B || !n || !out || n[0] < 1 || n[1] < 1 || n[2] < 1) return MARA_ERR_ARGUMENT;
+    if (bc != BC_PERIODIC && bc != BC_OUTFLOW) return MARA_ERR_CONFIG;
+    if (which == 0 && location != 0 && location != 1) return MARA_ERR_ARGUMENT;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    const long long cells = (long long) n[0] * n[1] * n[2];
+    const long long nout = which == 1 ? 3 * cells
+                           : location == 0 ? (long long) (n[0] + 1) * (n[1] + 1) * (n[2] + 1) : cells;
+    double *dB = nullptr, *dO = nullptr;
+    int rc = MARA_OK;
+    if (cudaMalloc(&dB, sizeof(double) * 3 * cells) != cudaSuccess ||
+        cudaMalloc(&dO, sizeof(double) * nout) != cudaSuccess ||
+        cudaMemcpy(dB, B, sizeof(double) * 3 * cells, cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = MARA_ERR_CUDA;
+    } else {
+        const UctField f{dB, n[0], n[1], n[2], bc};
+        const long long threads = which == 1 ? cells : nout;
+        const unsigned nb = (unsigned) ((threads + 255) / 256);
+        if (which == 0) k_uct_monopole<<<nb, 256>>>(f, location, dO);
+        else k_uct_current<<<nb, 256>>>(f, h, dO);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out, dO, sizeof(double) * nout, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = MARA_ERR_CUDA;
+    }
+    cudaFree(dB);
+    cudaFree(dO);
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}
+
+} // namespace mara
+
+extern "C" int mara_gpu_ct_monopole(const double* B, const int n[3], int bc, int location, double* M, int device)
+{
+    return mara::uct_call(B, n, bc, 0, location, 1.0, M, device);
+}
+
+extern "C" int mara_gpu_ct_current(const double* B, const int n[3], int bc, double mesh_spacing, double* J,
+                                   int device)
+{
+    return mara::uct_call(B, n, bc, 1, 0, mesh_spacing, J, device);
+}

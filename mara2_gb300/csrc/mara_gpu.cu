@@ -171,6 +171,87 @@ __global__ void k_generate(double* __restrict__ aos, GridDesc G, GenGeom geo, Ma
     for (int q = 0; q < G.nq; ++q) aos[c * G.nq + q] = P[q];
 }
 
+// ---- the divergence-free field from a vector potential (Problems.cpp:660-667)
+// A(face index n, component, face axis) over the (N + 1)^3 face index space
+struct VecPot {
+    const double* A;
+    int f0, f1, f2;
+    // CellCenteredFieldCT::vectorPotentialToFluxes (CellCenteredFieldCT.cpp:
+    // 136-150): flux of field component q through faces of axis a
+    __device__ __forceinline__ double F(int i, int j, int k, int q, int a) const
+    {
+        const double* p = A + (((long long) i * f1 + j) * f2 + k) * 9;
+        if (a == 0) return q == 1 ? -p[2 * 3 + 0] : q == 2 ? +p[1 * 3 + 0] : 0.0;
+        if (a == 1) return q == 2 ? -p[0 * 3 + 1] : q == 0 ? +p[2 * 3 + 1] : 0.0;
+        return q == 0 ? -p[1 * 3 + 2] : q == 1 ? +p[0 * 3 + 2] : 0.0;
+    }
+    // the fluxes after CellCenteredFieldCT::correctGodunovFluxes with magnetic
+    // index 0 (CellCenteredFieldCT.cpp:14-134): normal components zero, the
+    // tangential ones the edge-EMF average where the reference's loops reach
+    __device__ __forceinline__ double G(int i, int j, int k, int q, int a) const
+    {
+        if (q == a) return 0.0;
+        if (a == 0 && q == 1 && f0 >= 3 && i >= 1 && j >= 1 && j < f1 - 1)
+            return 0.125 * (+2 * F(i, j, k, 1, 0) + 1 * F(i, j + 1, k, 1, 0) + 1 * F(i, j - 1, k, 1, 0)
+                            - 1 * F(i, j + 1, k, 0, 1) - 1 * F(i - 1, j + 1, k, 0, 1)
+                            - 1 * F(i, j, k, 0, 1) - 1 * F(i - 1, j, k, 0, 1));
+        if (a == 0 && q == 2 && f0 >= 3 && i >= 1 && k >= 1 && k < f2 - 1)
+            return 0.125 * (+2 * F(i, j, k, 2, 0) + 1 * F(i, j, k + 1, 2, 0) + 1 * F(i, j, k - 1, 2, 0)
+                            - 1 * F(i, j, k + 1, 0, 2) - 1 * F(i - 1, j, k + 1, 0, 2)
+                            - 1 * F(i, j, k, 0, 2) - 1 * F(i - 1, j, k, 0, 2));
+        if (a == 1 && q == 2 && f1 >= 3 && j >= 1 && k >= 1 && k < f2 - 1)
+            return 0.125 * (+2 * F(i, j, k, 2, 1) + 1 * F(i, j, k + 1, 2, 1) + 1 * F(i, j, k - 1, 2, 1)
+                            - 1 * F(i, j, k + 1, 1, 2) - 1 * F(i, j - 1, k + 1, 1, 2)
+                            - 1 * F(i, j, k, 1, 2) - 1 * F(i, j - 1, k, 1, 2));
+        if (a == 1 && q == 0 && f1 >= 3 && i >= 1 && i < f0 - 1 && j >= 1)
+            return 0.125 * (+2 * F(i, j, k, 0, 1) + 1 * F(i + 1, j, k, 0, 1) + 1 * F(i - 1, j, k, 0, 1)
+                            - 1 * F(i + 1, j, k, 1, 0) - 1 * F(i + 1, j - 1, k, 1, 0)
+                            - 1 * F(i, j, k, 1, 0) - 1 * F(i, j - 1, k, 1, 0));
+        if (a == 2 && q == 0 && f2 >= 3 && i >= 1 && i < f0 - 1 && k >= 1)
+            return 0.125 * (+2 * F(i, j, k, 0, 2) + 1 * F(i + 1, j, k, 0, 2) + 1 * F(i - 1, j, k, 0, 2)
+                            - 1 * F(i + 1, j, k, 2, 0) - 1 * F(i + 1, j, k - 1, 2, 0)
+                            - 1 * F(i, j, k, 2, 0) - 1 * F(i, j, k - 1, 2, 0));
+        if (a == 2 && q == 1 && f2 >= 3 && j >= 1 && j < f1 - 1 && k >= 1)
+            return 0.125 * (+2 * F(i, j, k, 1, 2) + 1 * F(i, j + 1, k, 1, 2) + 1 * F(i, j - 1, k, 1, 2)
+                            - 1 * F(i, j + 1, k, 2, 1) - 1 * F(i, j + 1, k - 1, 2, 1)
+                            - 1 * F(i, j, k, 2, 1) - 1 * F(i, j, k - 1, 2, 1));
+        return F(i, j, k, q, a);
+    }
+};
+
+// Every cell of the AoS staging array (with guards): the magnetic field of
+// an interior cell becomes scale x MeshOperator::divergence(G, 1) there
+// (MeshOperator.cpp:323-381); a guard cell takes its boundary image's state
+// (applySimple: periodic wrap, outflow clamp, reflecting mirror with the
+// normal velocity negated), its field computed at the image.  Interior
+// threads write only the field components, guard threads read only the
+// others, so no thread reads what another writes.
+__global__ void k_assign_b(double* __restrict__ aos, GridDesc G, VecPot V, double scale)
+{
+    const long long total = (long long) G.N[0] * G.N[1] * G.N[2];
+    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;  // AoS order, k fastest
+    if (c >= total) return;
+    const int k = (int) (c % G.N[2]);
+    const int j = (int) ((c / G.N[2]) % G.N[1]);
+    const int i = (int) (c / ((long long) G.N[2] * G.N[1]));
+    int f[3] = {0, 0, 0};
+    const int ii = bc_interior(i, G.n[0], G.g[0], G.bc, f[0]) + G.g[0];
+    const int jj = bc_interior(j, G.n[1], G.g[1], G.bc, f[1]) + G.g[1];
+    const int kk = bc_interior(k, G.n[2], G.g[2], G.bc, f[2]) + G.g[2];
+    const double factor = 1.0;
+    const double vol = G.dV;
+    double* out = aos + c * G.nq;
+    for (int q = 0; q < 3; ++q)
+        out[5 + q] = factor / vol * (+V.G(ii + 1, jj, kk, q, 0) * G.dA[0] - V.G(ii, jj, kk, q, 0) * G.dA[0]
+                                     + V.G(ii, jj + 1, kk, q, 1) * G.dA[1] - V.G(ii, jj, kk, q, 1) * G.dA[1]
+                                     + V.G(ii, jj, kk + 1, q, 2) * G.dA[2] - V.G(ii, jj, kk, q, 2) * G.dA[2]) *
+                     scale;
+    if (ii == i && jj == j && kk == k) return;
+    const double* src = aos + (((long long) ii * G.N[1] + jj) * G.N[2] + kk) * G.nq;
+    for (int q = 0; q < G.nq; ++q)
+        if (q < 5 || q > 7) out[q] = (q >= 1 && q <= 3 && f[q - 1]) ? -src[q] : src[q];
+}
+
 void launch_courant_init(DevStatus* st, cudaStream_t s) { k_courant_init<<<1, 1, 0, s>>>(st); }
 void launch_dt_from_courant(DevStatus* st, double cfl, double t_final, cudaStream_t s)
 {
@@ -631,6 +712,41 @@ int mara_gpu_generate(MaraGpuHandle* h, const MaraInitialData* d)
     }
     h->launches++;
     return cuda_status(cudaGetLastError());
+}
+
+int mara_gpu_assign_vector_potential(MaraGpuHandle* h, const double* A, double scale)
+{
+    if (!h || !A) return MARA_ERR_ARGUMENT;
+    if (h->cfg.law != MARA_LAW_MHD && h->cfg.law != MARA_LAW_RMHD) return MARA_ERR_CONFIG;
+    CK(cudaSetDevice(h->cfg.device));
+    const VecPot shape{nullptr, h->G.N[0] + 1, h->G.N[1] + 1, h->G.N[2] + 1};
+    const size_t abytes = sizeof(double) * 9 * (size_t) shape.f0 * shape.f1 * shape.f2;
+    double* dA = nullptr;
+    CK(cudaMallocAsync(&dA, abytes, h->stream));
+    int rc = cuda_status(cudaMemcpyAsync(dA, A, abytes, cudaMemcpyHostToDevice, h->stream));
+    const long long total = h->G.sP;
+    if (rc == MARA_OK) {
+        // the resident state as FP64 primitives with guards, the field
+        // replaced, then loaded back like an upload
+        if (h->mixed) mixed_store_aos_range(h->mixed, h->stage_aos, 0, total, h->stream);
+        else launch_soa_to_aos_range(h->P[h->cur], h->stage_aos, h->G, 0, total, h->stream);
+        VecPot V = shape;
+        V.A = dA;
+        k_assign_b<<<(unsigned) ((total + 255) / 256), 256, 0, h->stream>>>(h->stage_aos, h->G, V, scale);
+        k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+        if (h->mixed) {
+            mixed_load_begin(h->mixed, h->stream);
+            mixed_load_aos_range(h->mixed, h->stage_aos, 0, total, h->st, h->stream);
+            mixed_load_finish(h->mixed, h->st, h->stream);
+        } else {
+            launch_aos_to_soa_range(h->stage_aos, h->P[h->cur], h->G, 0, total, h->stream);
+        }
+        h->launches += 4;
+        rc = cuda_status(cudaGetLastError());
+    }
+    const int rf = cuda_status(cudaFreeAsync(dA, h->stream));
+    if (rc == MARA_OK) rc = cuda_status(cudaStreamSynchronize(h->stream));
+    return rc != MARA_OK ? rc : rf;
 }
 
 int mara_gpu_download(MaraGpuHandle* h, double* P_aos)

@@ -196,8 +196,45 @@ class Solver:
                 "mara_gpu_field_diagnostics")
         return out
 
+    def assign_vector_potential(self, A: np.ndarray, scale: float = 1.0) -> None:
+        """The divergence-free field of src/Problems.cpp:660-667 from the
+        face-centred vector potential A (shape (N0+1, N1+1, N2+1, 3, 3)),
+        times scale, on the resident state (mara_gpu_assign_vector_potential)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        want = tuple(n + 1 for n in self.scheme.full_shape[:3]) + (3, 3)
+        if A.shape != want:
+            raise ValueError(f"vector potential shape {A.shape}, expected {want}")
+        N.check(self.lib.mara_gpu_assign_vector_potential(self.h, A.ctypes.data, scale),
+                "mara_gpu_assign_vector_potential")
+
     def kernel_times(self):
         ms = (C.c_double * 3)()
         n = (C.c_int64 * 3)()
         self.lib.mara_gpu_kernel_times(self.h, ms, n)
         return list(ms), list(n)
+
+
+_BC = {"periodic": 0, "outflow": 1, "reflecting": 2}
+
+
+def ct_monopole(B: np.ndarray, bc: str, location: str = "cell", device: int = 0) -> np.ndarray:
+    """UniformCartesianCT::computeMonopole (the ConstrainedTransport interface,
+    src/Mara.hpp:341-349) of a cell-centred field B (n0, n1, n2, 3) on the
+    device: at vertices ((n+1)^3) or cells (n^3)."""
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    n = np.array(B.shape[:3], dtype=np.int32)
+    M = np.zeros(tuple(int(m) + 1 for m in n) if location == "vert" else tuple(int(m) for m in n))
+    N.check(N.load().mara_gpu_ct_monopole(B.ctypes.data, n.ctypes.data, _BC[bc], 0 if location == "vert" else 1,
+                                          M.ctypes.data, device), "mara_gpu_ct_monopole")
+    return M
+
+
+def ct_current(B: np.ndarray, bc: str, mesh_spacing: float = 1.0, device: int = 0) -> np.ndarray:
+    """computeCurrent of the same adaptor (CellCenteredFieldCT::current of the
+    guarded field) at the interior cells: J (n0, n1, n2, 3)."""
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    n = np.array(B.shape[:3], dtype=np.int32)
+    J = np.zeros_like(B)
+    N.check(N.load().mara_gpu_ct_current(B.ctypes.data, n.ctypes.data, _BC[bc], mesh_spacing, J.ctypes.data,
+                                         device), "mara_gpu_ct_current")
+    return J

@@ -253,8 +253,13 @@ def face_vector_potential(s: Scheme, fn) -> np.ndarray:
     return A
 
 
-def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms: float = 0.5,
-                   rk_order: int = 3):
+def mhd_turbulence_parts(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms: float = 0.5,
+                         rk_order: int = 3):
+    """The MHD turbulence workload before its magnetic field is built: the
+    scheme, the state with B = 0, the face-centred vector potential A and the
+    factor that brings the rms of B over the interior to b_rms.  B follows
+    as scale x div(CT(fluxes of A)) (src/Problems.cpp:660-667), on the host
+    (mhd_turbulence) or on the device (Solver.assign_vector_potential)."""
     s = Scheme(law="mhd", recon="plm", riemann="hlle", bc="periodic", rk_order=rk_order,
                shape=(n, n, n), gamma=5.0 / 3, plm_theta=1.5, cfl=0.3, t_final=None, steps=100)
     P = empty_state(s)
@@ -270,6 +275,12 @@ def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms
     B = vector_potential_to_cell_b(s, A)
     inner_b = B[g:-g, g:-g, g:-g]
     scale = b_rms / math.sqrt(float(np.mean(np.sum(inner_b ** 2, axis=-1))))
+    return s, apply_bc_numpy(s, P), A, scale, B
+
+
+def mhd_turbulence(n: int = 256, seed: int = MHD_SEED, v_rms: float = 0.1, b_rms: float = 0.5,
+                   rk_order: int = 3):
+    s, P, A, scale, B = mhd_turbulence_parts(n, seed, v_rms, b_rms, rk_order)
     P[..., 5:8] = B * scale
     return s, apply_bc_numpy(s, P)
 

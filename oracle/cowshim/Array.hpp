@@ -236,6 +236,14 @@ public:
     double* data() { return D.data(); }
     const double* data() const { return D.data(); }
 
+    /** Copy the elements of `source` (a region of src) into the region
+        `target` of this array; both are walked in C order and must have the
+        same extents. */
+    void copyFrom (const Array& src, Region target, Region source)
+    {
+        Reference (*this, target) = Reference (const_cast<Array&> (src), source);
+    }
+
     Iterator begin() { return Iterator (data(), S, Region().absolute (S), false); }
     Iterator end() { return Iterator (data(), S, Region().absolute (S), true); }
 

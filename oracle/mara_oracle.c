@@ -1524,3 +1524,156 @@ void mo_current_cell(const double* B, int n0, int n1, int n2, double h, double* 
 #undef BI
 #undef JI
 }
+
+/* ------------------------------------------------------------------------ */
+/* UniformCartesianCT (src/ConstrainedTransport.cpp), the reference's only   */
+/* implementation of the ConstrainedTransport interface (src/Mara.hpp:341-  */
+/* 349): a cell-centred field with one guard zone on every axis             */
+/* (setMeshGeometry :13-76), filled by the boundary condition axis by axis  */
+/* (setCellBC :400-420; periodic and outflow images, numGuard = 1).         */
+/* ------------------------------------------------------------------------ */
+static double* uct_guarded_b(const double* Bc, int n0, int n1, int n2, int bc)
+{
+    const int m0 = n0 + 2, m1 = n1 + 2, m2 = n2 + 2;
+    double* B = (double*) calloc((size_t) m0 * m1 * m2 * 3, sizeof(double));
+    if (!B) return NULL;
+#define GB(i, j, k, c) B[(((long) (i) * m1 + (j)) * m2 + (k)) * 3 + (c)]
+    for (int i = 0; i < n0; ++i)
+        for (int j = 0; j < n1; ++j)
+            for (int k = 0; k < n2; ++k)
+                for (int c = 0; c < 3; ++c)
+                    GB(i + 1, j + 1, k + 1, c) = Bc[(((long) i * n1 + j) * n2 + k) * 3 + c];
+    const int n[3] = {n0, n1, n2};
+    for (int axis = 0; axis < 3; ++axis) {
+        /* left guard 0 and right guard n + 1 from their images: periodic
+         * n and 1, outflow 1 and n */
+        const int lsrc = bc == MO_BC_PERIODIC ? n[axis] : 1;
+        const int rsrc = bc == MO_BC_PERIODIC ? 1 : n[axis];
+        for (int a = 0; a < (axis == 0 ? 1 : m0); ++a)
+            for (int b = 0; b < (axis == 1 ? 1 : m1); ++b)
+                for (int e = 0; e < (axis == 2 ? 1 : m2); ++e)
+                    for (int c = 0; c < 3; ++c) {
+                        int gl[3] = {a, b, e}, gr[3] = {a, b, e}, sl[3] = {a, b, e}, sr[3] = {a, b, e};
+                        gl[axis] = 0;
+                        gr[axis] = n[axis] + 1;
+                        sl[axis] = lsrc;
+                        sr[axis] = rsrc;
+                        GB(gl[0], gl[1], gl[2], c) = GB(sl[0], sl[1], sl[2], c);
+                        GB(gr[0], gr[1], gr[2], c) = GB(sr[0], sr[1], sr[2], c);
+                    }
+    }
+#undef GB
+    return B;
+}
+
+int mo_uct_monopole(const double* Bc, int n0, int n1, int n2, int bc, int location, double* M)
+{
+    if (bc != MO_BC_PERIODIC && bc != MO_BC_OUTFLOW) return MO_ERR_CONFIG;
+    const int m1 = n1 + 2, m2 = n2 + 2;
+    const int v0 = n0 + 1, v1 = n1 + 1, v2 = n2 + 1;
+    double* B = uct_guarded_b(Bc, n0, n1, n2, bc);
+    double* Mv = (double*) calloc((size_t) v0 * v1 * v2, sizeof(double));
+    if (!B || !Mv) { free(B); free(Mv); return MO_ERR_CONFIG; }
+#define GB(i, j, k, c) B[(((long) (i) * m1 + (j)) * m2 + (k)) * 3 + (c)]
+#define MV(i, j, k) Mv[((long) (i) * v1 + (j)) * v2 + (k)]
+    /* computeMonopoleVert (ConstrainedTransport.cpp:302-356) */
+    for (int i = 0; i < v0; ++i)
+        for (int j = 0; j < v1; ++j)
+            for (int k = 0; k < v2; ++k) {
+                const double Bx0 = GB(i, j, k, 0) + GB(i, j, k + 1, 0) + GB(i, j + 1, k, 0) + GB(i, j + 1, k + 1, 0);
+                const double Bx1 = GB(i + 1, j, k, 0) + GB(i + 1, j, k + 1, 0) + GB(i + 1, j + 1, k, 0) + GB(i + 1, j + 1, k + 1, 0);
+                const double By0 = GB(i, j, k, 1) + GB(i + 1, j, k, 1) + GB(i, j, k + 1, 1) + GB(i + 1, j, k + 1, 1);
+                const double By1 = GB(i, j + 1, k, 1) + GB(i + 1, j + 1, k, 1) + GB(i, j + 1, k + 1, 1) + GB(i + 1, j + 1, k + 1, 1);
+                const double Bz0 = GB(i, j, k, 2) + GB(i, j + 1, k, 2) + GB(i + 1, j, k, 2) + GB(i + 1, j + 1, k, 2);
+                const double Bz1 = GB(i, j, k + 1, 2) + GB(i, j + 1, k + 1, 2) + GB(i + 1, j, k + 1, 2) + GB(i + 1, j + 1, k + 1, 2);
+                MV(i, j, k) = 0.25 * ((Bx1 - Bx0) + (By1 - By0) + (Bz1 - Bz0));
+            }
+    if (location == 0) {
+        memcpy(M, Mv, sizeof(double) * (size_t) v0 * v1 * v2);
+    } else {
+        /* computeMonopoleCell (ConstrainedTransport.cpp:358-377) */
+        for (int i = 0; i < n0; ++i)
+            for (int j = 0; j < n1; ++j)
+                for (int k = 0; k < n2; ++k) {
+                    const double Mi = 0.5 * (MV(i, j, k) + MV(i + 1, j, k));
+                    const double Mj = 0.5 * (MV(i, j, k) + MV(i, j + 1, k));
+                    const double Mk = 0.5 * (MV(i, j, k) + MV(i, j, k + 1));
+                    M[((long) i * n1 + j) * n2 + k] = 1. / 3 * (Mi + Mj + Mk);
+                }
+    }
+#undef GB
+#undef MV
+    free(B);
+    free(Mv);
+    return MO_OK;
+}
+
+int mo_uct_current(const double* Bc, int n0, int n1, int n2, int bc, double h, double* J)
+{
+    if (bc != MO_BC_PERIODIC && bc != MO_BC_OUTFLOW) return MO_ERR_CONFIG;
+    const int m0 = n0 + 2, m1 = n1 + 2, m2 = n2 + 2;
+    double* B = uct_guarded_b(Bc, n0, n1, n2, bc);
+    double* Jg = (double*) malloc(sizeof(double) * (size_t) m0 * m1 * m2 * 3);
+    if (!B || !Jg) { free(B); free(Jg); return MO_ERR_CONFIG; }
+    /* CellCenteredFieldCT::current (CellCenteredFieldCT.cpp:231-257) of the
+     * guarded field, kept at the interior cells */
+    mo_current_cell(B, m0, m1, m2, h, Jg);
+    for (int i = 0; i < n0; ++i)
+        for (int j = 0; j < n1; ++j)
+            for (int k = 0; k < n2; ++k)
+                for (int c = 0; c < 3; ++c)
+                    J[(((long) i * n1 + j) * n2 + k) * 3 + c] = Jg[(((long) (i + 1) * m1 + (j + 1)) * m2 + (k + 1)) * 3 + c];
+    free(B);
+    free(Jg);
+    return MO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The divergence-free initial field of src/Problems.cpp:660-667:           */
+/* CellCenteredFieldCT::vectorPotentialToFluxes (CellCenteredFieldCT.cpp:   */
+/* 136-150), generateGodunovFluxes (:152-157, flux CT with magnetic index   */
+/* 0), MeshOperator::divergence with factor 1 (MeshOperator.cpp:323-381),   */
+/* every cell with guards; each result times `scale`.  A has shape          */
+/* (N0+1, N1+1, N2+1, 3, 3) (component, face axis); B (N0, N1, N2, 3).       */
+/* ------------------------------------------------------------------------ */
+int mo_vector_potential_to_cell_b_scaled(const mo_config* c, const double* A, double scale, double* B)
+{
+    mgeom g;
+    int err = make_geom(c, &g);
+    if (err) return err;
+    const int f0 = g.N[0] + 1, f1 = g.N[1] + 1, f2 = g.N[2] + 1;
+    const long nf = (long) f0 * f1 * f2;
+    double* F = (double*) calloc((size_t) nf * 9, sizeof(double));
+    if (!F) return MO_ERR_CONFIG;
+#define AI(n, q, a) A[(n) * 9 + (q) * 3 + (a)]
+#define FX(n, q, a) F[(n) * 9 + (q) * 3 + (a)]
+    for (long n = 0; n < nf; ++n) {
+        FX(n, 1, 0) = -AI(n, 2, 0);
+        FX(n, 2, 0) = +AI(n, 1, 0);
+        FX(n, 2, 1) = -AI(n, 0, 1);
+        FX(n, 0, 1) = +AI(n, 2, 1);
+        FX(n, 0, 2) = -AI(n, 1, 2);
+        FX(n, 1, 2) = +AI(n, 0, 2);
+    }
+#undef AI
+    mo_ct_correct(F, f0, f1, f2, 3, 0);
+    const double factor = 1.0;
+    const double vol = g.dV;
+    for (int i = 0; i < g.N[0]; ++i)
+        for (int j = 0; j < g.N[1]; ++j)
+            for (int k = 0; k < g.N[2]; ++k) {
+#define FI(i, j, k) (((long) (i) * f1 + (j)) * f2 + (k))
+                for (int q = 0; q < 3; ++q)
+                    B[(((long) i * g.N[1] + j) * g.N[2] + k) * 3 + q] = factor / vol * (
+                        + FX(FI(i + 1, j, k), q, 0) * g.dA[0]
+                        - FX(FI(i, j, k), q, 0) * g.dA[0]
+                        + FX(FI(i, j + 1, k), q, 1) * g.dA[1]
+                        - FX(FI(i, j, k), q, 1) * g.dA[1]
+                        + FX(FI(i, j, k + 1), q, 2) * g.dA[2]
+                        - FX(FI(i, j, k), q, 2) * g.dA[2]) * scale;
+#undef FI
+            }
+#undef FX
+    free(F);
+    return MO_OK;
+}

@@ -136,6 +136,22 @@ int mo_volume_diagnostics(const mo_config* c, const double* P, double* D, double
  * data B (n0, n1, n2, 3); J has the same shape. */
 void mo_current_cell(const double* B, int n0, int n1, int n2, double mesh_spacing, double* J);
 
+/* UniformCartesianCT (src/ConstrainedTransport.cpp) on a cell-centred field
+ * Bc (n0, n1, n2, 3) given at the interior cells (assignCellCenteredB) with
+ * periodic or outflow guards: computeMonopole at vertices (location 0; M
+ * (n0+1, n1+1, n2+1)) or cells (location 1; M (n0, n1, n2)). */
+int mo_uct_monopole(const double* Bc, int n0, int n1, int n2, int bc, int location, double* M);
+
+/* The current operator of that adaptor: CellCenteredFieldCT::current
+ * (src/CellCenteredFieldCT.cpp:231-257) with mesh spacing h of the guarded
+ * field, at the interior cells; J (n0, n1, n2, 3). */
+int mo_uct_current(const double* Bc, int n0, int n1, int n2, int bc, double h, double* J);
+
+/* B = scale x divergence(CT(vectorPotentialToFluxes(A))) at every cell with
+ * guards (src/Problems.cpp:660-667); A (N0+1, N1+1, N2+1, 3, 3), B (N0, N1,
+ * N2, 3). */
+int mo_vector_potential_to_cell_b_scaled(const mo_config* c, const double* A, double scale, double* B);
+
 /* Face-normal unit vectors as CartesianMeshGeometry::faceNormal returns them
  * (UnitVector::xhat/yhat/zhat, src/UnitVector.cpp:9-11,32-39). */
 void mo_face_normals(double n[3][3]);

@@ -138,6 +138,9 @@ class Oracle:
         f("volume_diagnostics").argtypes = [cp, _D, _D, _D]
         f("current_cell").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_double, _D]
         f("current_cell").restype = None
+        f("uct_monopole").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D]
+        f("uct_current").argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _D]
+        f("vector_potential_to_cell_b_scaled").argtypes = [cp, _D, C.c_double, _D]
         if which == "port":
             L.mo_max_threads.restype = C.c_int
             L.mo_set_threads.argtypes = [C.c_int]
@@ -153,6 +156,27 @@ class Oracle:
         fail = Failure()
         status = self._f("advance")(C.byref(c), _ptr(P), t0, dt, C.byref(fail))
         return status, fail
+
+    def uct_monopole(self, B: np.ndarray, bc: str, location: str):
+        """UniformCartesianCT::computeMonopole of cell data B (n0, n1, n2, 3)."""
+        B = np.ascontiguousarray(B, dtype=float)
+        n = B.shape[:3]
+        M = np.zeros(tuple(m + 1 for m in n) if location == "vert" else n)
+        st = self._f("uct_monopole")(_ptr(B), *n, BC[bc], 0 if location == "vert" else 1, _ptr(M))
+        return st, M
+
+    def uct_current(self, B: np.ndarray, bc: str, h: float = 1.0):
+        B = np.ascontiguousarray(B, dtype=float)
+        J = np.zeros_like(B)
+        st = self._f("uct_current")(_ptr(B), *B.shape[:3], BC[bc], h, _ptr(J))
+        return st, J
+
+    def vector_potential_to_cell_b(self, c: Config, A: np.ndarray, scale: float = 1.0):
+        """B = scale x div(CT(fluxes of A)) at every cell with guards."""
+        A = np.ascontiguousarray(A, dtype=float)
+        B = np.zeros((A.shape[0] - 1, A.shape[1] - 1, A.shape[2] - 1, 3))
+        st = self._f("vector_potential_to_cell_b_scaled")(C.byref(c), _ptr(A), scale, _ptr(B))
+        return st, B
 
     def courant(self, c: Config, P: np.ndarray):
         dt = np.zeros(1)

@@ -19,6 +19,7 @@
 #include "IntercellFluxSchemes.hpp"
 #include "MeshData.hpp"
 #include "MeshOperator.hpp"
+#include "ConstrainedTransport.hpp"
 #include "QuarticPolynomial.hpp"
 #include "Reconstruction.hpp"
 #include "RiemannSolvers.hpp"
@@ -374,6 +375,69 @@ int mr_vector_potential_to_cell_b (const mo_config* c, const double* Aface, doub
         std::memcpy (Bcell, B.data(), sizeof (double) * B.size());
     )
     return status;
+}
+
+int mr_vector_potential_to_cell_b_scaled (const mo_config* c, const double* Aface, double scale, double* Bcell)
+{
+    const int status = mr_vector_potential_to_cell_b (c, Aface, Bcell);
+    if (status != MO_OK) return status;
+    auto s = make_setup (c);
+    auto bs = Cow::Shape3D (Cow::Shape {{c->ng[0], c->ng[1], c->ng[2], 0, 0}});
+    auto tot = Cow::Shape3D (s.mg->cellsShape()).increased (bs * 2);
+    const long n = (long) tot[0] * tot[1] * tot[2] * 3;
+    for (long m = 0; m < n; ++m) Bcell[m] = Bcell[m] * scale;
+    return MO_OK;
+}
+
+int mr_uct_current (const double* Bc, int n0, int n1, int n2, int bc, double h, double* J)
+{
+    // the guarded field as UniformCartesianCT::setCellBC fills it (one guard
+    // zone, axis by axis), then CellCenteredFieldCT::current at the interior
+    if (bc != MO_BC_PERIODIC && bc != MO_BC_OUTFLOW) return MO_ERR_CONFIG;
+    std::shared_ptr<BoundaryCondition> b;
+    if (bc == MO_BC_PERIODIC) b = std::make_shared<PeriodicBoundaryCondition>();
+    else b = std::make_shared<OutflowBoundaryCondition>();
+    auto Bg = Cow::Array (n0 + 2, n1 + 2, n2 + 2, 3);
+    for (int i = 0; i < n0; ++i)
+        for (int j = 0; j < n1; ++j)
+            for (int k = 0; k < n2; ++k)
+                for (int q = 0; q < 3; ++q)
+                    Bg (i + 1, j + 1, k + 1, q) = Bc[(((long) i * n1 + j) * n2 + k) * 3 + q];
+    for (int axis = 0; axis < 3; ++axis)
+    {
+        b->apply (Bg, MeshLocation::cell, MeshBoundary::left, axis, 1);
+        b->apply (Bg, MeshLocation::cell, MeshBoundary::right, axis, 1);
+    }
+    auto ct = CellCenteredFieldCT();
+    ct.setMeshSpacing (h);
+    auto Jg = ct.current (Bg, MeshLocation::cell);
+    for (int i = 0; i < n0; ++i)
+        for (int j = 0; j < n1; ++j)
+            for (int k = 0; k < n2; ++k)
+                for (int q = 0; q < 3; ++q)
+                    J[(((long) i * n1 + j) * n2 + k) * 3 + q] = Jg (i + 1, j + 1, k + 1, q);
+    return MO_OK;
+}
+
+int mr_uct_monopole (const double* Bc, int n0, int n1, int n2, int bc, int location, double* M)
+{
+    // UniformCartesianCT with a mesh geometry and a boundary condition; the
+    // field assigned at the interior cells, its monopole at vertices or cells
+    if (bc != MO_BC_PERIODIC && bc != MO_BC_OUTFLOW) return MO_ERR_CONFIG;
+    auto mg = std::make_shared<CartesianMeshGeometry>();
+    mg->setCellsShape (Cow::Shape {{n0, n1, n2, 1, 1}});
+    std::shared_ptr<BoundaryCondition> b;
+    if (bc == MO_BC_PERIODIC) b = std::make_shared<PeriodicBoundaryCondition>();
+    else b = std::make_shared<OutflowBoundaryCondition>();
+    auto ct = UniformCartesianCT();
+    ct.setMeshGeometry (mg);
+    ct.setBoundaryCondition (b);
+    auto B = Cow::Array (n0, n1, n2, 3);
+    std::memcpy (B.data(), Bc, sizeof (double) * B.size());
+    ct.assignCellCenteredB (B);
+    auto Mo = ct.computeMonopole (location == 0 ? MeshLocation::vert : MeshLocation::cell);
+    std::memcpy (M, Mo.data(), sizeof (double) * Mo.size());
+    return MO_OK;
 }
 
 void mr_set_source_terms (mo_source_fn fn, void* user)

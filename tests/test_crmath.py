@@ -52,7 +52,9 @@ def _eval(lib, name, fn, x, outs=2):
     n = len(x)
     ys = [np.empty(n) for _ in range(outs)]
     ptr = lambda a: a.ctypes.data_as(C.c_void_p)
-    rc = getattr(lib, name)(C.c_int(fn), ptr(x), C.c_int(n), *[ptr(y) for y in ys])
+    f = getattr(lib, name)
+    f.restype = None if name == "host_eval" else C.c_int
+    rc = f(C.c_int(fn), ptr(x), C.c_int(n), *[ptr(y) for y in ys])
     assert rc in (None, 0)
     return ys
 

@@ -222,3 +222,37 @@ def test_cooling_bitwise(port, ref, make, kw):
     assert A[..., 8].mean() > 0.02                      # energy moved into the auxiliary field
     a, b = port.volume_diagnostics(c, A), ref.volume_diagnostics(c, A)
     assert len(a[1]) == 18 and np.array_equal(_bits(a[1]), _bits(b[1]))
+
+
+@pytest.mark.parametrize("shape", [(6, 5, 4), (7, 6, 1), (9, 1, 1)])
+@pytest.mark.parametrize("bc", ["periodic", "outflow"])
+def test_uniform_cartesian_ct_bitwise(port, ref, shape, bc):
+    """UniformCartesianCT (the reference's ConstrainedTransport
+    implementation): monopole at vertices and cells of an assigned
+    cell-centred field, and the adaptor's current operator
+    (CellCenteredFieldCT::current of the guarded field)."""
+    rng = np.random.default_rng(sum(shape) + len(bc))
+    B = rng.standard_normal(shape + (3,))
+    for loc in ("vert", "cell"):
+        sa, Ma = port.uct_monopole(B, bc, loc)
+        sb, Mb = ref.uct_monopole(B, bc, loc)
+        assert sa == sb == 0
+        assert np.array_equal(_bits(Ma), _bits(Mb)), loc
+    sa, Ja = port.uct_current(B, bc, 0.25)
+    sb, Jb = ref.uct_current(B, bc, 0.25)
+    assert sa == sb == 0
+    assert np.array_equal(_bits(Ja), _bits(Jb))
+
+
+@pytest.mark.parametrize("make", [lambda: W.mhd_turbulence(6), lambda: W.rmhd_blast(10)])
+def test_vector_potential_to_cell_b_bitwise(port, ref, make):
+    """Problems.cpp:660-667 (fluxes of A -> flux CT -> divergence), every cell
+    with guards, then scaled."""
+    s, _ = make()
+    A = W.face_vector_potential(s, lambda x, y, z: W._fourier_vector(5, x, y, z))
+    c = oracle_config(s)
+    for scale in (1.0, 0.37):
+        sa, Ba = port.vector_potential_to_cell_b(c, A, scale)
+        sb, Bb = ref.vector_potential_to_cell_b(c, A, scale)
+        assert sa == sb == 0
+        assert np.array_equal(_bits(Ba), _bits(Bb))
