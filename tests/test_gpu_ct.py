@@ -6,7 +6,7 @@
   uploaded face-centred A, against the oracle (pinned bit for bit to the
   reference build): the same bits on the plain path, the FP32-pair
   round-off on the mixed path, and a plain step taken from it equal to the
-  oracle's step.
+  oracle's step (bit for bit, or within 1e-12 per field for RMHD).
 * The ConstrainedTransport interface (src/Mara.hpp:341-349) as
   UniformCartesianCT implements it: monopole at vertices and cells, and the
   adaptor's current, bit for bit against the oracle.
@@ -14,7 +14,7 @@
 import numpy as np
 import pytest
 
-from helpers import oracle_config
+from helpers import oracle_config, rel_l1
 from mara2_gb300 import workloads as W
 from mara2_gb300.solver import Solver, ct_current, ct_monopole
 
@@ -71,7 +71,13 @@ def test_assign_vector_potential_plain_matches_oracle(gpu_lib, port, name, s, P,
     st, _ = port.advance(oracle_config(s), ref, dt)
     assert st == 0
     i = s.interior()
-    assert np.array_equal(_bits(stepped[i]), _bits(ref[i])), name
+    if s.law == "rmhd":
+        # the quartic's pow / acos / cos / sin: correctly rounded on the
+        # device, the host's libm on all but ~0.1 % of arguments
+        err = rel_l1(stepped[i], ref[i])
+        assert np.all(err <= 1e-12), (name, err.tolist())
+    else:
+        assert np.array_equal(_bits(stepped[i]), _bits(ref[i])), name
 
 
 @pytest.mark.gpu
