@@ -43,9 +43,15 @@ enum { MARA_WENO_JS96 = 0, MARA_WENO_BORGES08 = 1, MARA_WENO_SHENZHA10 = 2 };
 /* arithmetic of the step */
 enum {
     MARA_PRECISION_FP64 = 0,  /* plain: matches the reference's FP64 CPU path  */
-    MARA_PRECISION_MIXED = 1  /* FP32 reconstruction/Riemann/flux arithmetic,
-                                 compensated FP32 pair (hi+lo) conserved-state
-                                 accumulator, FP64 RMHD Newton iteration      */
+    MARA_PRECISION_MIXED = 1, /* FP32 reconstruction/Riemann/flux arithmetic,
+                                 compensated FP32 pair (hi+lo, ~48 bits)
+                                 conserved-state accumulator; RMHD recovery
+                                 with its Newton residuals in FP32 pairs and
+                                 the FP64 iteration as fallback               */
+    MARA_PRECISION_MIXED_FP64 = 2 /* FP32 reconstruction/Riemann/flux
+                                 arithmetic, FP64 conserved-state accumulator
+                                 and FP64 RMHD Newton iteration (the same 8
+                                 bytes per field as the pair)                 */
 };
 
 /* Status codes.  1..8 mirror ConsToPrimRMHD's enum (src/ConsToPrimRMHD.hpp:
@@ -328,6 +334,12 @@ int mara_gpu_ct_current(const double* B, const int n[3], int bc, double mesh_spa
  * condition (applyBoundaryCondition).  MHD and RMHD handles, either
  * precision; the arithmetic is FP64 and gives the reference's bits. */
 int mara_gpu_assign_vector_potential(MaraGpuHandle* h, const double* A, double scale);
+
+/* The FP64 pipe's throughput in TFLOP/s (one FMA counted as two flops),
+ * measured with independent FMA chains in every thread of eight CTAs per SM:
+ * the ceiling the plain FP64 path's arithmetic runs against.  No counterpart
+ * in the reference; the benchmark reports the plain path against it. */
+int mara_gpu_fp64_peak(int device, double* tflops);
 
 /* QuarticPolynomial::solve (src/QuarticPolynomial.cpp:19-144) on the device
  * for n quartics d4 x^4 + d3 x^3 + d2 x^2 + d1 x + d0: coeffs (host) holds

@@ -17,7 +17,7 @@ RECON = {"pcm": 0, "plm": 1, "weno5": 2}
 RIEMANN = {"hlle": 0, "hllc": 1}
 BC = {"periodic": 0, "outflow": 1, "reflecting": 2}
 WENO_IS = {"js96": 0, "borges08": 1, "shenzha10": 2}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_fp64": 2}
 
 MARA_OK = 0
 MARA_ERR_INVERSION_FAILURE = 16
@@ -101,6 +101,7 @@ SIGNATURES = {
     "mara_gpu_ct_monopole": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]),
     "mara_gpu_ct_current": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_int]),
     "mara_gpu_assign_vector_potential": (C.c_int, [_H, C.c_void_p, C.c_double]),
+    "mara_gpu_fp64_peak": (C.c_int, [C.c_int, _D]),
     "mara_gpu_advance_noalloc": (C.c_int, [C.POINTER(MaraGpuConfig), C.c_void_p, C.c_void_p, C.c_double,
                                            C.c_void_p]),
 }

@@ -173,12 +173,13 @@ class ServeResult:
                 "peak_active_grids": self.peak_active, "peak_bytes": self.peak_bytes}
 
 
-def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bool = False,
+def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results=False,
           max_grids: int = 4096, tile_1d: int = 0, tile_2d: int = 0, device: int = 0, make=None,
           lockstep_1d: bool = False) -> ServeResult:
     """Continuous batching of `requests` (objects with .arrival seconds and a
     way to build (Scheme, P) through `make(req)`), arrivals replayed against
-    the wall clock."""
+    the wall clock.  keep_results: True keeps every result, a set of request
+    indices keeps those."""
     from . import workloads as W
     make = make or W.riemann_initial
     pending = deque(sorted(requests, key=lambda r: r.arrival))
@@ -216,7 +217,7 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results: bo
                     res.zone_updates += s.zones * nsteps
                     res.completed += 1
                     res.records.append((r.index, done_t - r.arrival, t_admit - r.arrival, nsteps))
-                    if keep_results:
+                    if keep_results is True or (keep_results and r.index in keep_results):
                         res.results[r.index] = (out, t, nsteps)
                 st = b.stats()
                 res.peak_active = max(res.peak_active, st.active)

@@ -274,3 +274,64 @@ extern "C" int mara_gpu_ct_current(const double* B, const int n[3], int bc, doub
 {
     return mara::uct_call(B, n, bc, 1, 0, mesh_spacing, J, device);
 }
+
+// ---- the FP64 pipe's throughput ---------------------------------------------------
+namespace mara {
+
+// eight independent FMA chains per thread; the result is kept live by a
+// store that never happens (the sum is never that value)
+__global__ void __launch_bounds__(256) k_dfma_peak(double* out, int iters, double a, double b)
+{
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = __fma_rn(x[k], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == -1.0) out[0] = s;
+}
+
+} // namespace mara
+
+extern "C" int mara_gpu_fp64_peak(int device, double* tflops)
+{
+    using namespace mara;
+    if (!tflops) return MARA_ERR_ARGUMENT;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) return MARA_ERR_NO_DEVICE;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = MARA_OK;
+    if (cudaMalloc(&out, sizeof(double)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        rc = MARA_ERR_CUDA;
+    } else {
+        float best = 0.0f;
+        for (int rep = 0; rep < 4; ++rep) {  // the first launch warms up
+            cudaEventRecord(e0);
+            k_dfma_peak<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7);
+            cudaEventRecord(e1);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = MARA_ERR_CUDA; break; }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && (best == 0.0f || ms < best)) best = ms;
+        }
+        if (rc == MARA_OK && cudaGetLastError() == cudaSuccess && best > 0.0f)
+            *tflops = 2.0 * 8.0 * (double) iters * blocks * threads / (best * 1e-3) / 1e12;
+        else if (rc == MARA_OK)
+            rc = MARA_ERR_CUDA;
+    }
+    cudaFree(out);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}

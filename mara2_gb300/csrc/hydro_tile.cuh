@@ -11,11 +11,13 @@
 //      momentum negated), axis by axis as applySimple composes them;
 //   2. x-face fluxes, then y-face fluxes (reconstruction + fromPrimitive x2
 //      + Riemann solver) into shared memory;
-//   3. per zone: divergence, the RK combine on the FP32-pair accumulator,
-//      store; on the last stage also the zone's Courant time step.
+//   3. per zone: divergence, the RK combine on the FP32-pair accumulator
+//      (or, with ACC64, on an FP64 accumulator), store; on the last stage
+//      also the zone's Courant time step.
 // The state lives only as conserved densities (no primitive or flux arrays
 // in HBM), so a stage moves 8 bytes per field per zone for each of: the
-// stage input, U0 (stages after the first) and the output.
+// stage input, U0 (stages after the first) and the output, with either
+// accumulator.
 #pragma once
 
 #include "physics_fp32.cuh"
@@ -23,8 +25,8 @@
 namespace mara {
 
 struct HGrid {
-    float* Uh[3];      // FP32-pair conserved densities, SoA, 5 fields
-    float* Ul[3];
+    float* Uh[3];      // FP32-pair conserved densities, SoA, 5 fields (with an
+    float* Ul[3];      // FP64 accumulator: Uh holds the doubles, Ul unused)
     long long sU;      // field stride (n0 * n1)
     int n0, n1;        // interior zones (n1 = 1 for 1-D)
     int bc;
@@ -278,12 +280,45 @@ __device__ __forceinline__ float ld_state(const float* p)
     else return *p;
 }
 
+// The stage input's FP32 value of field element idx: the high word of the
+// pair (hi = the pair's value rounded to FP32), or the FP64 accumulator
+// rounded to FP32 (ACC64: the array holds doubles).
+template <bool L2ONLY, bool ACC64>
+__device__ __forceinline__ float ld_u32(const float* base, long long idx)
+{
+    if constexpr (ACC64) {
+        const double* p = reinterpret_cast<const double*>(base) + idx;
+        return __double2float_rn(L2ONLY ? __ldcg(p) : *p);
+    } else {
+        return ld_state<L2ONLY>(base + idx);
+    }
+}
+
+// RK weight b of SolutionSchemes.cpp:135-138 in FP64 from its FP32 form
+// (1, 1/2, 1/4 or 2/3)
+__device__ __forceinline__ double rk_b_fp64(float b)
+{
+    return b == 1.0f ? 1.0 : b == 0.5f ? 0.5 : b == 0.25f ? 0.25 : 2.0 / 3.0;
+}
+
+// U_new = U0 (1 - b) + (U + dt L) b (SolutionSchemes.cpp:232-235) on the FP64
+// accumulator; dt L is the FP32 flux arithmetic's product, exact in FP64
+__device__ __forceinline__ double rk_combine_d(double U0, double U, float dtL, float b)
+{
+    const double s = __dadd_rn(U, (double) dtL);
+    if (b == 1.0f) return s;
+    if (b == 0.5f) return __dmul_rn(0.5, __dadd_rn(U0, s));
+    const double bd = rk_b_fp64(b);
+    return __dadd_rn(__dmul_rn(U0, __dsub_rn(1.0, bd)), __dmul_rn(s, bd));
+}
+
 // One RK stage of one tile of grid g whose state is in rotation buffer s:
 //   src: buffer holding the stage input; dst: buffer written; buffer s
 //   holds U0 (read per zone); b, omb = b, 1 - b; on the last stage the
 //   tile's Courant step goes to *at.cfl().  at.dt() and at.cfl() are read
 //   where they are used, so that neither holds registers across the tile.
-template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, class At>
+//   ACC64: the state arrays (Uh) hold the FP64 accumulator, Ul is unused.
+template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, class At>
 __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, const HGrid& g, const TileRef& tr,
                                            int s, int stage, float b, float omb, int last, const At& at)
 {
@@ -306,15 +341,16 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     // after the first stage, both words of U0
     {
         const int rows = DIM == 2 ? TY : 1;
-        const int per = (TX * 4 + 127) / 128;            // 128-byte lines per row segment
-        const int arrays = stage == 0 ? 1 : 3;
+        constexpr int W = ACC64 ? 8 : 4;                 // bytes per element
+        const int per = (TX * W + 127) / 128;            // 128-byte lines per row segment
+        const int arrays = ACC64 ? (stage == 0 ? 0 : 1) : (stage == 0 ? 1 : 3);
         const int lines = arrays * 5 * rows * per;
         for (int l = threadIdx.x; l < lines; l += NT) {
             const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
-            const int y = tr.y0 + r, x = tr.x0 + seg * 32;
+            const int y = tr.y0 + r, x = tr.x0 + seg * (128 / W);
             if (y < n1 && x < n0) {
-                const float* base = a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
-                const float* ptr = base + q * sU + (long long) y * n0 + x;
+                const float* base = ACC64 ? g.Uh[s] : a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
+                const char* ptr = reinterpret_cast<const char*>(base) + ((long long) q * sU + (long long) y * n0 + x) * W;
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
             }
         }
@@ -332,16 +368,16 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
         const bool inner = tr.x0 - G >= 0 && tr.x0 + TX + G <= n0 &&
                            (DIM == 1 || (tr.y0 - G >= 0 && tr.y0 + TY + G <= n1));
         if (inner) {
-            const float* base = Uin + (long long) (tr.y0 - (DIM == 2 ? G : 0)) * n0 + (tr.x0 - G);
+            const long long base = (long long) (tr.y0 - (DIM == 2 ? G : 0)) * n0 + (tr.x0 - G);
 #pragma unroll
             for (int k = 0; k < NC; ++k) {
                 const int c = threadIdx.x + k * NT;
                 fl[k] = 0;
                 if (c < WX * WY) {
                     const int lx = c % WX, ly = c / WX;
-                    const float* p = base + (long long) ly * n0 + lx;
+                    const long long p = base + (long long) ly * n0 + lx;
 #pragma unroll
-                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(p + q * sU);
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_u32<L2ONLY, ACC64>(Uin, p + q * sU);
                 }
             }
         } else {
@@ -356,7 +392,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                     const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, n1, g.bc, flipy) : 0;
                     const long long o = (long long) y * n0 + x;
 #pragma unroll
-                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(Uin + q * sU + o);
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_u32<L2ONLY, ACC64>(Uin, q * sU + o);
                     fl[k] = flipx | (flipy << 1);
                 }
             }
@@ -436,12 +472,21 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                 L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx, sm.Fy[q][ly][lx], sm.Fy[q][ly + 1][lx], idy);
             else
                 L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx);
-            const df U0 = {ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
-            const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
-            const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
-            Unh[q * sU + o] = Un.hi;
-            Unl[q * sU + o] = Un.lo;
-            Unew[q] = Un.hi;
+            if constexpr (ACC64) {
+                const double* U0d = reinterpret_cast<const double*>(U0h) + q * sU + o;
+                const double* Upd = reinterpret_cast<const double*>(Uph) + q * sU + o;
+                const double u0 = b == 1.0f ? 0.0 : (L2ONLY ? __ldcg(U0d) : *U0d);
+                const double Un = rk_combine_d(u0, L2ONLY ? __ldcg(Upd) : *Upd, f_mul(dt, L), b);
+                reinterpret_cast<double*>(Unh)[q * sU + o] = Un;
+                Unew[q] = __double2float_rn(Un);
+            } else {
+                const df U0 = {ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
+                const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
+                const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
+                Unh[q * sU + o] = Un.hi;
+                Unl[q * sU + o] = Un.lo;
+                Unew[q] = Un.hi;
+            }
         }
         if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
     }
@@ -449,7 +494,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
 }
 
 // One RK stage over a list of tiles (persistent: CTAs stride over tiles).
-template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT>
+template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool ACC64 = false>
 __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict__ grids,
                                                         const TileRef* __restrict__ tiles,
                                                         const int* __restrict__ ntiles_p,
@@ -471,7 +516,7 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
             __device__ float dt() const { return (float) *dtp; }
             __device__ unsigned long long* cfl() const { return slot; }
         } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride};
-        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
+        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
     }
 }
 

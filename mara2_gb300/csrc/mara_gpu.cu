@@ -369,7 +369,9 @@ static int validate(const MaraGpuConfig* c)
     if (c->law < 0 || c->law > 2 || s == 0 || c->riemann < 0 || c->riemann > 1 || c->bc < 0 || c->bc > 2)
         return MARA_ERR_CONFIG;
     if (c->rk_order < 1 || c->rk_order > 3) return MARA_ERR_CONFIG;
-    if (c->precision != MARA_PRECISION_FP64 && c->precision != MARA_PRECISION_MIXED) return MARA_ERR_CONFIG;
+    if (c->precision != MARA_PRECISION_FP64 && c->precision != MARA_PRECISION_MIXED &&
+        c->precision != MARA_PRECISION_MIXED_FP64)
+        return MARA_ERR_CONFIG;
     if (c->law == MARA_LAW_MHD && c->cooling_rate > 0.0 && c->precision != MARA_PRECISION_FP64)
         return MARA_ERR_CONFIG;  // the auxiliary field is on the plain path only
     static_assert(CONV_MAXQ >= 9, "the layout conversions stage up to 9 fields per cell");

@@ -348,30 +348,14 @@ __device__ __forceinline__ bool rm_recover_pair(const GridF& G, const df* U, con
     return true;
 }
 
-// primitive recovery of the mixed path: FP32 for hydro and MHD; for RMHD the
-// pair-residual Newton iteration above, else the FP64 ConsToPrimRMHD solve
-template <int LAW>
-__device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code, const float* Pprev = nullptr)
+// the relativistic recovery's FP64 ConsToPrimRMHD solve (ConsToPrimRMHD.cpp:
+// 183-323) from FP64 conserved densities
+__device__ __forceinline__ int recover_rmhd_fp64(const GridF& G, const double* U, float* P, int* code,
+                                                 const float* Pprev)
 {
-    constexpr int NQ = LawInfo<LAW>::NQ;
-    if constexpr (LAW == LAW_HYDRO) {
-        float U[5];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) U[q] = Un[q].hi + Un[q].lo;
-        hydro_cons_f(G.gamma, U, P);
-        return ST_OK;
-    } else if constexpr (LAW == LAW_MHD) {
-        float U[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) U[q] = Un[q].hi + Un[q].lo;
-        const int e = mhd_cons_f(G.gamma, G.pressure_floor, U, P);
-        *code = e;
-        return e;
-    } else {
-        if (rm_recover_pair(G, Un, Pprev, P)) return ST_OK;
-        double U[NQ], Pd[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) U[q] = df_to_double(Un[q]);
+    constexpr int NQ = 8;
+    {
+        double Pd[NQ];
         PhysParams pp;
         pp.gamma = G.gamma_d;
         pp.pressure_floor = G.pfloor_d;
@@ -420,6 +404,57 @@ __device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float
     }
 }
 
+// FP32 recovery of hydro and MHD from FP32 conserved densities
+template <int LAW>
+__device__ __forceinline__ int recover_f32(const GridF& G, const float* U, float* P, int* code)
+{
+    if constexpr (LAW == LAW_HYDRO) {
+        hydro_cons_f(G.gamma, U, P);
+        return ST_OK;
+    } else {
+        const int e = mhd_cons_f(G.gamma, G.pressure_floor, U, P);
+        *code = e;
+        return e;
+    }
+}
+
+// primitive recovery of the mixed path: FP32 for hydro and MHD; for RMHD the
+// pair-residual Newton iteration above, else the FP64 ConsToPrimRMHD solve
+template <int LAW>
+__device__ __forceinline__ int recover_mixed(const GridF& G, const df* Un, float* P, int* code, const float* Pprev = nullptr)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    if constexpr (LAW != LAW_RMHD) {
+        float U[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) U[q] = Un[q].hi + Un[q].lo;
+        return recover_f32<LAW>(G, U, P, code);
+    } else {
+        if (rm_recover_pair(G, Un, Pprev, P)) return ST_OK;
+        double U[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) U[q] = df_to_double(Un[q]);
+        return recover_rmhd_fp64(G, U, P, code, Pprev);
+    }
+}
+
+// the recovery with the FP64 accumulator: FP32 for hydro and MHD (from the
+// accumulator rounded to FP32), the FP64 Newton solve for RMHD
+template <int LAW>
+__device__ __forceinline__ int recover_acc64(const GridF& G, const double* Un, float* P, int* code,
+                                             const float* Pprev = nullptr)
+{
+    constexpr int NQ = LawInfo<LAW>::NQ;
+    if constexpr (LAW != LAW_RMHD) {
+        float U[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) U[q] = __double2float_rn(Un[q]);
+        return recover_f32<LAW>(G, U, P, code);
+    } else {
+        return recover_rmhd_fp64(G, Un, P, code, Pprev);
+    }
+}
+
 // Courant step of one zone from its FP32 primitives: lmin / the largest
 // |eigenvalue| over the three face normals (FieldOperator::getCourantTimestep,
 // FieldOperator.cpp:125-169); an eigenvalue error goes to the status
@@ -445,7 +480,7 @@ __device__ __forceinline__ float zone_dt_f(const GridF& G, const float* P, DevSt
 // stage input and output may be one array, RK1).  Eight blocks per SM: the
 // kernel is bound by memory latency, and 32 resident warps with a few spilled
 // registers beat 20 warps without (MHD 256^3: 2.34e9 -> 2.64e9 zone-updates/s).
-template <int LAW>
+template <int LAW, bool ACC64>
 __global__ void __launch_bounds__(128, 8) update_f_kernel(float* __restrict__ Pf, const float* U0h, const float* U0l,
                                                        const float* Uph, const float* Upl, float* Unh, float* Unl,
                                                        FluxViewF V, GridF G,
@@ -466,15 +501,22 @@ __global__ void __launch_bounds__(128, 8) update_f_kernel(float* __restrict__ Pf
     if (active) {
         const float dt = (float) *dtp;
         const bool fx = G.n[0] > 1, fy = G.n[1] > 1, fz = G.n[2] > 1;
-        df U0[NQ], Up[NQ];
+        // FP32 pairs, or FP64 (ACC64: the arrays Uh hold doubles)
+        using Acc = std::conditional_t<ACC64, double, df>;
+        Acc U0[NQ], Up[NQ];
         float L[NQ];
         // the zone's previous primitives: the RMHD recovery's starting point,
         // and what a failed recovery keeps (read only then for the other laws)
         float Pold[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-            U0[q] = {U0h[q * G.sU + uc], U0l[q * G.sU + uc]};
-            Up[q] = {Uph[q * G.sU + uc], Upl[q * G.sU + uc]};
+            if constexpr (ACC64) {
+                U0[q] = reinterpret_cast<const double*>(U0h)[q * G.sU + uc];
+                Up[q] = reinterpret_cast<const double*>(Uph)[q * G.sU + uc];
+            } else {
+                U0[q] = {U0h[q * G.sU + uc], U0l[q * G.sU + uc]};
+                Up[q] = {Uph[q * G.sU + uc], Upl[q * G.sU + uc]};
+            }
             if constexpr (LAW == LAW_RMHD) Pold[q] = Pf[q * G.sP + pc];
         }
 #pragma unroll
@@ -485,16 +527,25 @@ __global__ void __launch_bounds__(128, 8) update_f_kernel(float* __restrict__ Pf
             if (fz) l -= (face_flux_f<NQ>(V, G, 2, q, i, j, k + 1) - face_flux_f<NQ>(V, G, 2, q, i, j, k)) * G.idx[2];
             L[q] = l;
         }
-        df Un[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) Un[q] = rk_combine(U0[q], Up[q], dt * L[q], b, omb);
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            Unh[q * G.sU + uc] = Un[q].hi;
-            Unl[q * G.sU + uc] = Un[q].lo;
-        }
+        Acc Un[NQ];
         int code = ST_OK;
-        const int e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
+        int e;
+        if constexpr (ACC64) {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) Un[q] = rk_combine_d(U0[q], Up[q], dt * L[q], b);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) reinterpret_cast<double*>(Unh)[q * G.sU + uc] = Un[q];
+            e = recover_acc64<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
+        } else {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) Un[q] = rk_combine(U0[q], Up[q], dt * L[q], b, omb);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                Unh[q * G.sU + uc] = Un[q].hi;
+                Unl[q * G.sU + uc] = Un[q].lo;
+            }
+            e = recover_mixed<LAW>(G, Un, Pn, &code, LAW == LAW_RMHD ? Pold : nullptr);
+        }
         if (e == ST_INVERSION_FAILURE) {
             atomicAdd(&st->failures, 1);
             const unsigned long long z = (unsigned long long) uc;
@@ -572,7 +623,7 @@ __global__ void __launch_bounds__(256) courant_f_kernel(const float* __restrict_
 // per-cell accesses are slow) and transposed to cells in shared memory.
 constexpr int CONV_BLOCK = 256;
 
-template <int LAW>
+template <int LAW, bool ACC64>
 __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restrict__ aos, long long c0, long long c1,
                                                           float* Uh, float* Ul, float* Pf, GridF G, PhysParams pp,
                                                           DevStatus* st, unsigned long long* cfl)
@@ -609,10 +660,15 @@ __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restri
             float hi[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
-                const df d = df_from_double(U[q]);
-                Uh[q * G.sU + u] = d.hi;
-                Ul[q * G.sU + u] = d.lo;
-                hi[q] = d.hi;
+                if constexpr (ACC64) {
+                    reinterpret_cast<double*>(Uh)[q * G.sU + u] = U[q];
+                    hi[q] = __double2float_rn(U[q]);
+                } else {
+                    const df d = df_from_double(U[q]);
+                    Uh[q * G.sU + u] = d.hi;
+                    Ul[q * G.sU + u] = d.lo;
+                    hi[q] = d.hi;
+                }
             }
             // the Courant step from the stored high words, as the last RK
             // stage computes it
@@ -625,7 +681,7 @@ __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restri
 
 // FP64 primitives of cell c (AoS order) from the FP32-pair state; a guard
 // zone is the boundary image of an interior zone
-template <int LAW, bool L2ONLY = false>
+template <int LAW, bool L2ONLY = false, bool ACC64 = false>
 __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, long long c, const GridF& G,
                                            const PhysParams& pp, double* out)
 {
@@ -640,8 +696,10 @@ __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, lon
     const long long u = ((long long) kk * G.n[1] + jj) * G.n[0] + ii;
     double U[NQ], P[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q)
-        U[q] = (double) ld_state<L2ONLY>(Uh + q * G.sU + u) + (double) ld_state<L2ONLY>(Ul + q * G.sU + u);
+    for (int q = 0; q < NQ; ++q) {
+        if constexpr (ACC64) U[q] = reinterpret_cast<const double*>(Uh)[q * G.sU + u];
+        else U[q] = (double) ld_state<L2ONLY>(Uh + q * G.sU + u) + (double) ld_state<L2ONLY>(Ul + q * G.sU + u);
+    }
     if constexpr (LAW == LAW_HYDRO) {
         hydro_u2p_d(U, G.gm1_d, P);
     } else {
@@ -657,7 +715,7 @@ __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, lon
 
 // FP32-pair state -> AoS FP64 primitives with guards, cells [c0, c1), each
 // block's slab written as one contiguous run
-template <int LAW>
+template <int LAW, bool ACC64>
 __global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, const float* Ul, double* __restrict__ aos,
                                                            long long c0, long long c1, GridF G, PhysParams pp)
 {
@@ -665,7 +723,7 @@ __global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, cons
     __shared__ double slab[CONV_BLOCK * NQ];
     const long long b0 = c0 + blockIdx.x * (long long) CONV_BLOCK;
     const int nc = (int) min((long long) CONV_BLOCK, c1 - b0);
-    if (threadIdx.x < nc) store_cell<LAW>(Uh, Ul, b0 + threadIdx.x, G, pp, &slab[threadIdx.x * NQ]);
+    if (threadIdx.x < nc) store_cell<LAW, false, ACC64>(Uh, Ul, b0 + threadIdx.x, G, pp, &slab[threadIdx.x * NQ]);
     __syncthreads();
     for (int e = threadIdx.x; e < nc * NQ; e += CONV_BLOCK) aos[b0 * NQ + e] = slab[e];
 }
@@ -718,6 +776,7 @@ struct MixedState {
     GridF GF;
     PhysParams pp;
     bool fused = false;
+    bool acc64 = false;      // MARA_PRECISION_MIXED_FP64: Uh hold FP64 accumulators
     float* Uh[3] = {nullptr, nullptr, nullptr};
     float* Ul[3] = {nullptr, nullptr, nullptr};
     float* Pf = nullptr;
@@ -780,11 +839,16 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
     m->pp.pressure_floor = c->pressure_floor; m->pp.weno_is = c->weno_is;
 
     m->fused = c->law == MARA_LAW_HYDRO && G.n[2] == 1 && c->recon != MARA_RECON_WENO5 && G.n[0] > 1;
+    m->acc64 = c->precision == MARA_PRECISION_MIXED_FP64;
     const int nq = G.nq;
     int rc = MARA_OK;
     for (int b = 0; b < 3 && !rc; ++b) {
-        rc = dev_alloc((void**) &m->Uh[b], sizeof(float) * G.sU * nq, s, bytes);
-        if (!rc) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
+        if (m->acc64) {
+            rc = dev_alloc((void**) &m->Uh[b], sizeof(double) * G.sU * nq, s, bytes);
+        } else {
+            rc = dev_alloc((void**) &m->Uh[b], sizeof(float) * G.sU * nq, s, bytes);
+            if (!rc) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
+        }
     }
     if (!rc) rc = dev_alloc((void**) &m->drot, sizeof(int), s, bytes);
     if (!rc) rc = dev_alloc((void**) &m->dcfl, sizeof(unsigned long long), s, bytes);
@@ -881,24 +945,33 @@ void mixed_load_begin(MixedState* m, cudaStream_t s)
     k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl);
 }
 
-void mixed_load_aos_range(MixedState* m, const double* aos, long long c0, long long c1, DevStatus* st, cudaStream_t s)
+template <bool ACC64>
+static void load_range(MixedState* m, const double* aos, long long c0, long long c1, DevStatus* st, cudaStream_t s)
 {
-    if (c1 <= c0) return;
     const int r = host_rot(m);
     const unsigned nb = (unsigned) ((c1 - c0 + 255) / 256);
     switch (m->cfg.law) {
         case MARA_LAW_HYDRO:
             // the fused form reduces the first Courant step here
-            load_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st,
-                                                      m->fused ? m->dcfl : nullptr);
+            load_kernel<LAW_HYDRO, ACC64><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st,
+                                                             m->fused ? m->dcfl : nullptr);
             break;
         case MARA_LAW_MHD:
-            load_kernel<LAW_MHD><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st, nullptr);
+            load_kernel<LAW_MHD, ACC64><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st,
+                                                           nullptr);
             break;
         default:
-            load_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st, nullptr);
+            load_kernel<LAW_RMHD, ACC64><<<nb, 256, 0, s>>>(aos, c0, c1, m->Uh[r], m->Ul[r], m->Pf, m->GF, m->pp, st,
+                                                            nullptr);
             break;
     }
+}
+
+void mixed_load_aos_range(MixedState* m, const double* aos, long long c0, long long c1, DevStatus* st, cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    if (m->acc64) load_range<true>(m, aos, c0, c1, st, s);
+    else load_range<false>(m, aos, c0, c1, st, s);
 }
 
 void mixed_load_finish(MixedState* m, DevStatus* st, cudaStream_t s)
@@ -908,22 +981,35 @@ void mixed_load_finish(MixedState* m, DevStatus* st, cudaStream_t s)
     if (!m->fused) courant_general(m, st, s);
 }
 
-void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s)
+template <bool ACC64>
+static void store_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s)
 {
-    if (c1 <= c0) return;
     const unsigned nb = (unsigned) ((c1 - c0 + 255) / 256);
     const int r = host_rot(m);
     switch (m->cfg.law) {
-        case MARA_LAW_HYDRO: store_kernel<LAW_HYDRO><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
-        case MARA_LAW_MHD: store_kernel<LAW_MHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
-        default: store_kernel<LAW_RMHD><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp); break;
+        case MARA_LAW_HYDRO:
+            store_kernel<LAW_HYDRO, ACC64><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp);
+            break;
+        case MARA_LAW_MHD:
+            store_kernel<LAW_MHD, ACC64><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp);
+            break;
+        default:
+            store_kernel<LAW_RMHD, ACC64><<<nb, 256, 0, s>>>(m->Uh[r], m->Ul[r], aos, c0, c1, m->GF, m->pp);
+            break;
     }
+}
+
+void mixed_store_aos_range(MixedState* m, double* aos, long long c0, long long c1, cudaStream_t s)
+{
+    if (c1 <= c0) return;
+    if (m->acc64) store_range<true>(m, aos, c0, c1, s);
+    else store_range<false>(m, aos, c0, c1, s);
 }
 
 // ---- diagnostics ---------------------------------------------------------------
 // interior zone (i, j, k) of the FP32-pair state, converted to FP64
 // primitives exactly as a download converts it
-template <int LAW>
+template <int LAW, bool ACC64>
 struct MixedSrc {
     const float* Uh;
     const float* Ul;
@@ -937,7 +1023,10 @@ struct MixedSrc {
         const long long u = ((long long) k * n1 + j) * n0 + i;
         double U[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) U[q] = (double) Uh[q * sU + u] + (double) Ul[q * sU + u];
+        for (int q = 0; q < NQ; ++q) {
+            if constexpr (ACC64) U[q] = reinterpret_cast<const double*>(Uh)[q * sU + u];
+            else U[q] = (double) Uh[q * sU + u] + (double) Ul[q * sU + u];
+        }
         if constexpr (LAW == LAW_HYDRO) {
             hydro_u2p_d(U, gm1, P);
             return ST_OK;
@@ -949,11 +1038,11 @@ struct MixedSrc {
     }
 };
 
-template <int LAW>
+template <int LAW, bool ACC64>
 static void volume_diag_mixed(MixedState* m, double* partial, int* err, double* out, cudaStream_t s)
 {
     const int r = host_rot(m);
-    const MixedSrc<LAW> src{m->Uh[r], m->Ul[r], m->GF.sU, m->G.n[0], m->G.n[1], m->GF.gm1_d, m->pp};
+    const MixedSrc<LAW, ACC64> src{m->Uh[r], m->Ul[r], m->GF.sU, m->G.n[0], m->G.n[1], m->GF.gm1_d, m->pp};
     const long long zones = (long long) m->G.n[0] * m->G.n[1] * m->G.n[2];
     const long long want = (zones + 255) / 256;
     const int nb = (int) (want < DIAG_BLOCKS ? want : DIAG_BLOCKS);
@@ -963,10 +1052,18 @@ static void volume_diag_mixed(MixedState* m, double* partial, int* err, double* 
 
 void mixed_volume_diagnostics(MixedState* m, double* partial, int* err, double* out, cudaStream_t s)
 {
+    if (m->acc64) {
+        switch (m->cfg.law) {
+            case MARA_LAW_HYDRO: volume_diag_mixed<LAW_HYDRO, true>(m, partial, err, out, s); break;
+            case MARA_LAW_MHD: volume_diag_mixed<LAW_MHD, true>(m, partial, err, out, s); break;
+            default: volume_diag_mixed<LAW_RMHD, true>(m, partial, err, out, s); break;
+        }
+        return;
+    }
     switch (m->cfg.law) {
-        case MARA_LAW_HYDRO: volume_diag_mixed<LAW_HYDRO>(m, partial, err, out, s); break;
-        case MARA_LAW_MHD: volume_diag_mixed<LAW_MHD>(m, partial, err, out, s); break;
-        default: volume_diag_mixed<LAW_RMHD>(m, partial, err, out, s); break;
+        case MARA_LAW_HYDRO: volume_diag_mixed<LAW_HYDRO, false>(m, partial, err, out, s); break;
+        case MARA_LAW_MHD: volume_diag_mixed<LAW_MHD, false>(m, partial, err, out, s); break;
+        default: volume_diag_mixed<LAW_RMHD, false>(m, partial, err, out, s); break;
     }
 }
 
@@ -1055,10 +1152,18 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
         dim3 grid((m->G.n[0] + 127) / 128, m->G.n[1], m->G.n[2]);
         timed(m, s, [&] {
 #define MARA_UPDATE_ARGS m->Pf, m->Uh[sb], m->Ul[sb], m->Uh[src], m->Ul[src], m->Uh[dst], m->Ul[dst], V, m->GF, dt, b, 1.f - b, done, st, cfl
-            switch (m->cfg.law) {
-                case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                case MARA_LAW_MHD: update_f_kernel<LAW_MHD><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                default: update_f_kernel<LAW_RMHD><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+            if (m->acc64) {
+                switch (m->cfg.law) {
+                    case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_MHD: update_f_kernel<LAW_MHD, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    default: update_f_kernel<LAW_RMHD, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                }
+            } else {
+                switch (m->cfg.law) {
+                    case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_MHD: update_f_kernel<LAW_MHD, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    default: update_f_kernel<LAW_RMHD, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                }
             }
 #undef MARA_UPDATE_ARGS
         });
@@ -1071,8 +1176,12 @@ template <int DIM, int RECON, int RIEMANN>
 static void tile_launch(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int stage, float b, int last)
 {
     constexpr int TX = DIM == 2 ? 32 : 256, TY = DIM == 2 ? 16 : 1, NT = 256;
-    hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT><<<m->ctas, NT, 0, s>>>(
-        m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+    if (m->acc64)
+        hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT, true><<<m->ctas, NT, 0, s>>>(
+            m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+    else
+        hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT><<<m->ctas, NT, 0, s>>>(
+            m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
 }
 
 template <int DIM>
@@ -1379,7 +1488,7 @@ bool mixed_host_step_capable(const MixedState* m)
     // pipeline's fixed costs outweigh the overlap (256^2: 0.098 ms against
     // 0.085 ms unpipelined; 512^2 even; 1024^2 0.45 against 0.56 ms)
     const int rx = m->G.n[0] % 32, ry = m->G.n[1] % 16;
-    return m->fused && m->G.n[1] > 1 && m->G.N[2] == 1 && m->G.n[0] >= 128 && m->tx == 32 && m->ty == 16 &&
+    return m->fused && !m->acc64 && m->G.n[1] > 1 && m->G.N[2] == 1 && m->G.n[0] >= 128 && m->tx == 32 && m->ty == 16 &&
            (rx == 0 || rx >= 2) && (ry == 0 || ry >= 2) && (long long) m->G.n[0] * m->G.n[1] >= (1 << 19) &&
            !m->hs_unavailable;
 }
@@ -1601,7 +1710,7 @@ bool mixed_fused(const MixedState* m) { return m->fused; }
 // ---- small 1-D grids: many steps per launch on one thread-block cluster -------
 bool mixed_cluster_capable(const MixedState* m)
 {
-    return m->fused && m->G.n[1] == 1 && m->G.n[2] == 1 &&
+    return m->fused && !m->acc64 && m->G.n[1] == 1 && m->G.n[2] == 1 &&
            m->G.n[0] <= CLUSTER1D_MAX_CTAS * CLUSTER1D_MAX_ZONES_PER_CTA;
 }
 

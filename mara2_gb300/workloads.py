@@ -406,3 +406,52 @@ def device_initial_data(name: str, n: int = None, req: RiemannRequest = None):
         return s, {"kind": MARA_INIT_PLANAR_RIEMANN, "left": req.left, "right": req.right, "x0": (0.5, 0.5, 0.5),
                    "normal": nrm}
     raise ValueError(name)
+
+
+# ----------------------------------------------------------------------------
+# conserved densities of a primitive array (for error reports)
+# ----------------------------------------------------------------------------
+CONSERVED_NAMES = {
+    "hydro": ["density", "momentum1", "momentum2", "momentum3", "energy"],
+    "mhd": ["density", "momentum1", "momentum2", "momentum3", "energy", "magnetic1", "magnetic2", "magnetic3"],
+    "rmhd": ["density", "momentum1", "momentum2", "momentum3", "energy", "magnetic1", "magnetic2", "magnetic3"],
+}
+
+
+def conserved(s: Scheme, P: np.ndarray) -> np.ndarray:
+    """U of every zone of P (..., nq) by the law's fromPrimitive
+    (NewtonianHydro ConservationLaws.cpp:253-290, NewtonianMHD :416-447,
+    RelativisticMHD :659-720), in numpy FP64."""
+    P = np.asarray(P, dtype=np.float64)
+    U = np.empty_like(P)
+    rho, v, p = P[..., 0], P[..., 1:4], P[..., 4]
+    gm1 = s.gamma - 1.0
+    vv = np.sum(v * v, axis=-1)
+    if s.law == "hydro":
+        U[..., 0] = rho
+        U[..., 1:4] = rho[..., None] * v
+        U[..., 4] = rho * 0.5 * vv + p / gm1
+    elif s.law == "mhd":
+        B = P[..., 5:8]
+        U[..., 0] = rho
+        U[..., 1:4] = rho[..., None] * v
+        U[..., 4] = rho * 0.5 * vv + 0.5 * np.sum(B * B, axis=-1) + p / gm1
+        U[..., 5:] = P[..., 5:]
+    else:
+        B = P[..., 5:8]
+        BB = np.sum(B * B, axis=-1)
+        Bv = np.sum(B * v, axis=-1)
+        W2 = 1.0 / (1.0 - vv)
+        W0 = np.sqrt(W2)
+        b0 = W0 * Bv
+        bb = (BB + b0 * b0) / W2
+        b = (B + (b0 * W0)[..., None] * v) / W0[..., None]
+        e0 = (p / rho) / gm1
+        es = e0 + 0.5 * bb / rho
+        ps = p + 0.5 * bb
+        hs = 1.0 + es + ps / rho
+        U[..., 0] = rho * W0
+        U[..., 4] = rho * hs * W2 - ps - b0 * b0 - U[..., 0]
+        U[..., 1:4] = (rho * hs * W2)[..., None] * v - b0[..., None] * b
+        U[..., 5:8] = B
+    return U

@@ -31,6 +31,24 @@ def test_kh1024_plain_matches_oracle_bitwise(gpu_lib, port):
 
 
 @pytest.mark.gpu
+def test_sod1024_plain_matches_oracle_to_t_final(gpu_lib, port):
+    """configs[0] in full: Sod 1024 to t = 0.2, the driver loop on the
+    device (dt = CFL x Courant, clipped to t_final) against the oracle's
+    loop: the same number of steps, the same clock and the same bits."""
+    s, P = W.sod(1024)
+    ref = P.copy()
+    status, t_ref, dts = port.run(oracle_config(s), ref, 100_000, s.cfl, s.t_final)
+    assert status == 0 and abs(t_ref - s.t_final) < 1e-12
+    with Solver(s, "fp64") as g:
+        g.upload(P.copy())
+        n = g.run(100_000, s.cfl, s.t_final)
+        out = g.download()
+        assert g.t == t_ref
+    assert n == len(dts)
+    assert np.array_equal(out[s.interior()].view(np.uint64), ref[s.interior()].view(np.uint64))
+
+
+@pytest.mark.gpu
 def test_rmhd512_mixed_close_to_oracle(gpu_lib, port):
     s, P = W.rmhd_blast(512)
     ref = P.copy()

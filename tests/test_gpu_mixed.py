@@ -1,7 +1,7 @@
 """Mixed-precision path against the FP64 oracle.
 
-FP32 reconstruction / Riemann / flux arithmetic with an FP32-pair conserved
-accumulator must stay within the stated tolerance of the FP64 reference on
+FP32 reconstruction / Riemann / flux arithmetic with an FP32-pair (or FP64)
+conserved accumulator must stay within the stated tolerance of the FP64 reference on
 the same inputs and the same dt sequence: relative L1 density error <= 1e-5
 (the precision contract), checked here over short runs where it is met with
 a wide margin, for every law and both kernel families."""
@@ -64,13 +64,16 @@ CASES = _cases()
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp64"])
 @pytest.mark.parametrize("name,s,P,steps", CASES, ids=[c[0] for c in CASES])
-def test_mixed_close_to_fp64_oracle(gpu_lib, port, name, s, P, steps):
+def test_mixed_close_to_fp64_oracle(gpu_lib, port, name, s, P, steps, precision):
+    """Both mixed recipes: the FP32-pair accumulator, and the FP64
+    accumulator with the FP64 RMHD Newton solve."""
     c = oracle_config(s)
     ref = P.copy()
     status, _, dts = port.run(c, ref, steps, s.cfl, s.t_final)
     assert status == 0
-    with Solver(s, "mixed") as g:
+    with Solver(s, precision) as g:
         g.upload(P.copy())
         for dt in dts:
             g.advance(dt)
