@@ -88,13 +88,19 @@ def plain_roofline(ms_step, zones, nq, rk, peak_hbm, device):
     tf = C.c_double(0.0)
     rc = N.load().mara_gpu_fp64_peak(device, C.byref(tf))
     flops = _profile_value("plain_fp64_kh.txt", "fp64_flops_per_zone_update")
+    insts = _profile_value("plain_fp64_kh.txt", "fp64_pipe_inst_per_zone_update")
     out = {"hbm": {"achieved": hbm, "peak": peak_hbm, "unit": "GB/s", "frac": hbm / peak_hbm,
                    "algorithmic_bytes_per_zone_update": per_zone},
            "fp64_pipe": {"peak_tflops_measured": tf.value if rc == 0 else None,
-                         "flops_per_zone_update": flops,
-                         "achieved_tflops": rate * flops / 1e12 if flops else None}}
+                         "flops_per_zone_update": flops, "pipe_inst_per_zone_update": insts,
+                         "achieved_tflops": rate * flops / 1e12 if flops else None,
+                         "source": "per-zone FP64 counts from profiles/plain_fp64_kh.txt (ncu), "
+                                   "peak from independent DFMA chains timed here"}}
     if rc == 0 and flops:
-        out["fp64_pipe"]["frac"] = out["fp64_pipe"]["achieved_tflops"] / tf.value
+        out["fp64_pipe"]["frac_flops"] = out["fp64_pipe"]["achieved_tflops"] / tf.value
+    if rc == 0 and insts:
+        # one FMA instruction = two flops: the pipe's instruction rate is half the flop rate
+        out["fp64_pipe"]["frac_pipe_issue"] = rate * insts / (tf.value * 1e12 / 2)
     return out
 
 
@@ -291,12 +297,50 @@ def e2e(solver, P0, steps: int, warmup: int):
     return (t1 - t0) * 1e3 / steps, nbytes, solver.stats().kernel_launches - launches0
 
 
+def _ref_worker(args):
+    """One host process: the reference's own advance (its hot-path sources
+    compiled in place, serial as the reference is) on its own copy of the
+    workload, whole steps until the time budget is spent."""
+    n_side, budget_s = args
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from mara2_gb300 import workloads as W
+    s, P = W.kelvin_helmholtz(n_side)
+    ref = O.Oracle("ref")
+    c = O.make_config(law=s.law, recon=s.recon, riemann=s.riemann, bc=s.bc, rk_order=s.rk_order,
+                      shape=s.shape, lower=s.lower, upper=s.upper, gamma=s.gamma, plm_theta=s.plm_theta)
+    _, dtc = ref.courant(c, P)
+    dt = s.cfl * dtc
+    n, t0 = 0, time.perf_counter()
+    while True:
+        st, _ = ref.advance(c, P, dt)
+        n += 1
+        if st or time.perf_counter() - t0 > budget_s:
+            break
+    return n, time.perf_counter() - t0
+
+
 def cpu_baseline(s, P0, budget_s: float = 20.0):
-    """The oracle (C restatement of the reference's advance, OpenMP over zones)
-    on the host cores: whole KH steps until the time budget is spent."""
+    """The reference's algorithm on the host cores.  Where its own hot-path
+    sources built on this host (oracle/_ref, from the staged source tree), one
+    serial process per host core, each advancing its own copy of the
+    workload (the reference parallelises only by MPI ranks, absent here);
+    else the oracle restatement with OpenMP over zones."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build(False)
+    if O.ref_available():
+        import multiprocessing as mp
+        procs = os.cpu_count() or 1
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_ref_worker, [(s.shape[0], budget_s)] * procs)
+        steps = sum(n for n, _ in res)
+        wall = max(t for _, t in res)
+        return {"value": s.zones * steps / wall, "unit": UNIT, "cores": procs, "kind": "reference",
+                "sample": f"{steps} whole steps of the {s.shape[0]}x{s.shape[1]} KH workload over {wall:.1f} s: "
+                          f"the reference's own sources (compiled in place, g++ -O2 -ffp-contract=off), one "
+                          f"serial process per host core, each on its own copy of the grid"}
     port = O.Oracle("port")
     c = O.make_config(law=s.law, recon=s.recon, riemann=s.riemann, bc=s.bc, rk_order=s.rk_order,
                       shape=s.shape, lower=s.lower, upper=s.upper, gamma=s.gamma, plm_theta=s.plm_theta)
@@ -402,10 +446,13 @@ RECIPES = {"mixed": "FP32 flux arithmetic, FP32-pair (~48-bit) accumulator, RMHD
            "mixed_fp64": "FP32 flux arithmetic, FP64 accumulator, FP64 RMHD Newton iteration"}
 
 
-def config_run(name, s, P0, device, t_final=None, steps=None, extra=None):
+def config_run(name, s, P0, device, t_final=None, steps=None, extra=None, control=False):
     """One workload at its stated length: the plain FP64 path (the reference's
     arithmetic) and both mixed recipes, the recipes' per-field error against
-    the plain path on the plain path's dt sequence, failure counts."""
+    the plain path on the plain path's dt sequence, failure counts.  With
+    control, also the plain path itself from the initial state moved by one
+    unit in the last place in every zone's density (same dt sequence): how
+    far round-off alone carries the solution apart over the run."""
     out = {"zones": s.zones, "length": f"t = {t_final}" if t_final is not None else f"{steps} steps"}
     t0 = time.perf_counter()
     ref, dts, ms, fail = run_plain_recorded(s, P0, device, t_final, steps)
@@ -424,6 +471,14 @@ def config_run(name, s, P0, device, t_final=None, steps=None, extra=None):
             entry.update(extra(res))
         out[prec] = entry
         del res
+    if control:
+        P1 = P0.copy()
+        P1[..., 0] = np.nextafter(P1[..., 0], np.inf)
+        res, _ = run_replayed(s, P1, "fp64", dts, device)
+        out["fp64_one_ulp_control"] = {
+            "perturbation": "initial density + 1 ulp in every zone (guards alike), plain FP64, same dt sequence",
+            "error_vs_plain_fp64": field_errors(s, res, ref)}
+        del res, P1
     out["wall_s"] = time.perf_counter() - t0
     del ref
     return out
@@ -499,7 +554,7 @@ def workload_suite(device: int, serving_requests: int = 4096):
 
     # configs[1]: Kelvin-Helmholtz 1024^2 to t = 1.0
     s, P0 = W.kelvin_helmholtz(1024)
-    out["kh_1024_t1.0"] = config_run("kh", s, P0, device, t_final=1.0)
+    out["kh_1024_t1.0"] = config_run("kh", s, P0, device, t_final=1.0, control=True)
 
     # configs[2]: MHD turbulence with CT, 256^3, RK3, 100 steps
     s, P0 = W.mhd_turbulence(256)
@@ -520,7 +575,7 @@ def workload_suite(device: int, serving_requests: int = 4096):
 
     # configs[3]: relativistic MHD blast 512^2 to t = 4.0
     s, P0 = W.rmhd_blast(512)
-    out["rmhd_blast_512_t4.0"] = config_run("rmhd", s, P0, device, t_final=4.0)
+    out["rmhd_blast_512_t4.0"] = config_run("rmhd", s, P0, device, t_final=4.0, control=True)
 
     # configs[4]: the serving stream
     out["serving_riemann_4096"] = serving_suite(device, requests=serving_requests)
@@ -550,9 +605,8 @@ def main():
     dist, rank, ws, local = _dist()
 
     if args.impl == "reference":
-        # the reference's algorithm on the host cores (the oracle restatement:
-        # the reference's own build needs its source tree, absent on the GPU
-        # host); rank 0 only
+        # the reference's own CPU implementation on the host cores (rank 0
+        # only; no GPU work in this process, so the spawned workers start clean)
         if rank != 0:
             return
         cb = cpu_baseline(s, P0, args.cpu_budget)
