@@ -496,19 +496,19 @@ def serving_suite(device, requests=4096, rate=2000.0, sample=8, budget_gb=96.0):
     reqs = W.riemann_stream(requests, rate=rate)
     rng = np.random.default_rng(20261204)
     pick = sorted(int(i) for i in rng.choice(len(reqs), size=sample, replace=False))
-    res = serve(reqs, budget_bytes=int(budget_gb * (1 << 30)), tile_1d=tiles["tile_1d"], tile_2d=tiles["tile_2d"],
-                device=device, keep_results=set(pick))
+    form = {"tile_1d": tiles["tile_1d"], "tile_2d": tiles["tile_2d"], "persistent": tiles["persistent"],
+            "ctas_per_sm": tiles["ctas_per_sm"]}
+    res = serve(reqs, budget_bytes=int(budget_gb * (1 << 30)), device=device, keep_results=set(pick), **form)
     out = {"stream": f"{requests} Riemann problems (1-D N log-uniform [256, 8192], 2-D side log-uniform "
                      f"[128, 512]), Poisson {rate}/s, t = 0.2, PLM + HLLC, RK2, seed {W.RIEMANN_SEED}",
-           "saturated": res.summary(), "tiles": {"tile_1d": tiles["tile_1d"], "tile_2d": tiles["tile_2d"]},
+           "saturated": res.summary(), "launch_form": form, "autotune": tiles,
            "budget_bytes": int(budget_gb * (1 << 30))}
     # below saturation: the same distribution at half the measured capacity
     zu_mean = res.zone_updates / max(1, res.completed)
     cap = res.summary()["zone_updates_per_s"] / zu_mean
     sub_rate = 0.5 * cap
     sub = W.riemann_stream(512, rate=sub_rate, seed=W.RIEMANN_SEED + 7)
-    r2 = serve(sub, budget_bytes=int(budget_gb * (1 << 30)), tile_1d=tiles["tile_1d"], tile_2d=tiles["tile_2d"],
-               device=device)
+    r2 = serve(sub, budget_bytes=int(budget_gb * (1 << 30)), device=device, **form)
     out["below_saturation"] = {**r2.summary(), "rate_per_s": sub_rate,
                                "offered_load": "half the saturated stream's capacity (requests/s)"}
     # each sampled request alone: plain FP64 (the configs' baseline) and mixed

@@ -32,7 +32,8 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotu
 class MaraBatchConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_int64), ("max_grids", C.c_int),
                 ("max_zones_per_grid", C.c_int), ("recon", C.c_int), ("riemann", C.c_int),
-                ("rk_order", C.c_int), ("tile_1d", C.c_int), ("tile_2d", C.c_int), ("lockstep_1d", C.c_int)]
+                ("rk_order", C.c_int), ("tile_1d", C.c_int), ("tile_2d", C.c_int), ("lockstep_1d", C.c_int),
+                ("persistent", C.c_int), ("ctas_per_sm", C.c_int)]
 
 
 class MaraBatchStats(C.Structure):
@@ -51,6 +52,7 @@ SIGNATURES = {
     "mara_batch_retire": (C.c_int, [_H, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "mara_batch_stats": (C.c_int, [_H, C.POINTER(MaraBatchStats)]),
     "mara_batch_tiles": (C.c_int, [_H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mara_batch_launch_form": (C.c_int, [_H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }
 
 
@@ -66,13 +68,15 @@ def load():
 class Batch:
     def __init__(self, budget_bytes: int, max_grids: int = 4096, max_zones_per_grid: int = 600 * 600,
                  recon: str = "plm", riemann: str = "hllc", rk_order: int = 2, tile_1d: int = 0,
-                 tile_2d: int = 0, device: int = 0, lockstep_1d: bool = False):
+                 tile_2d: int = 0, device: int = 0, lockstep_1d: bool = False, persistent: bool = False,
+                 ctas_per_sm: int = 0):
         self.lib = load()
         c = MaraBatchConfig()
         c.device, c.hbm_budget_bytes, c.max_grids = device, int(budget_bytes), max_grids
         c.max_zones_per_grid, c.recon, c.riemann = max_zones_per_grid, N.RECON[recon], N.RIEMANN[riemann]
         c.rk_order, c.tile_1d, c.tile_2d = rk_order, tile_1d, tile_2d
         c.lockstep_1d = int(lockstep_1d)
+        c.persistent, c.ctas_per_sm = int(persistent), ctas_per_sm
         self.cfg = c
         h = C.c_void_p()
         N.check(self.lib.mara_batch_create(C.byref(c), C.byref(h)), "mara_batch_create")
@@ -135,6 +139,13 @@ class Batch:
         self.lib.mara_batch_tiles(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
 
+    def launch_form(self):
+        """(persistent, CTAs): one cooperative launch per step call, or the
+        per-stage launches."""
+        a, b = C.c_int(), C.c_int()
+        self.lib.mara_batch_launch_form(self.h, C.byref(a), C.byref(b))
+        return bool(a.value), b.value
+
 
 def run_alone(s: Scheme, P: np.ndarray, t_final: float, **kw):
     """One request by itself in a batch (the reference form of the invariance
@@ -175,7 +186,7 @@ class ServeResult:
 
 def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results=False,
           max_grids: int = 4096, tile_1d: int = 0, tile_2d: int = 0, device: int = 0, make=None,
-          lockstep_1d: bool = False) -> ServeResult:
+          lockstep_1d: bool = False, persistent: bool = False, ctas_per_sm: int = 0) -> ServeResult:
     """Continuous batching of `requests` (objects with .arrival seconds and a
     way to build (Scheme, P) through `make(req)`), arrivals replayed against
     the wall clock.  keep_results: True keeps every result, a set of request
@@ -188,7 +199,8 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results=Fal
     res = ServeResult()
     max_cells = max(int(np.prod(make(r)[0].full_shape[:3])) for r in [max(requests, key=lambda r: r.zones())])
     with Batch(budget_bytes, max_grids=max_grids, max_zones_per_grid=max_cells, tile_1d=tile_1d,
-               tile_2d=tile_2d, device=device, lockstep_1d=lockstep_1d) as b:
+               tile_2d=tile_2d, device=device, lockstep_1d=lockstep_1d, persistent=persistent,
+               ctas_per_sm=ctas_per_sm) as b:
         t0 = time.perf_counter()
         while pending or queue or inflight:
             now = time.perf_counter() - t0
@@ -230,37 +242,55 @@ def serve(requests, budget_bytes: int, steps_per_poll: int = 8, keep_results=Fal
 
 # ----------------------------------------------------------------------------
 def autotune(device: int = 0, sample: int = 48, steps: int = 40, force: bool = False) -> dict:
-    """Time every tile-shape candidate on a representative mix of the Riemann
-    workload (1-D and 2-D grids of the stream's size distribution) and cache
-    the fastest per dimension."""
+    """Time the launch configurations on a representative mix of the
+    Riemann workload (grids of the stream's size distribution) and cache the
+    fastest: the 1-D tile (128 / 256 / 512 zones, 1-D grids in the tile
+    lists), then for the 2-D grids the launch form - per-stage launches with
+    each 2-D tile shape (32x8, 32x16, 64x8), or the persistent cooperative
+    launch with each tile shape it supports (32x8, 32x16) and 2, 3 or 4 CTAs
+    per SM."""
     if not force and os.path.exists(CACHE):
         with open(CACHE) as f:
-            return json.load(f)
+            best = json.load(f)
+        if "persistent" in best:
+            return best
     import torch
     from . import workloads as W
     reqs = W.riemann_stream(sample, seed=W.RIEMANN_SEED + 1)
     grids = [W.riemann_initial(r) for r in reqs]
-    best = {}
-    for dim, cands in ((1, (128, 256, 512)), (2, (1, 2, 3))):
-        sel = [(s, P) for s, P in grids if s.dims == dim]
+
+    def time_batch(sel, **kw):
         zones = sum(s.zones for s, _ in sel)
-        timing = {}
-        for cand in cands:
-            kw = {"tile_1d": cand} if dim == 1 else {"tile_2d": cand}
-            with Batch(budget_bytes=200 * zones + (1 << 26), max_grids=len(sel) + 1,
-                       max_zones_per_grid=max(int(np.prod(s.full_shape[:3])) for s, _ in sel), device=device,
-                       **kw) as b:
-                for s, P in sel:
-                    b.admit(s, P, 1e9)
-                b.step(3)
-                b.poll()
-                torch.cuda.synchronize(device)
-                t0 = time.perf_counter()
-                b.step(steps)
-                b.poll()
-                timing[cand] = (time.perf_counter() - t0) / steps
-        best[f"tile_{dim}d"] = min(timing, key=timing.get)
-        best[f"timing_{dim}d_ms"] = {str(k): v * 1e3 for k, v in timing.items()}
+        with Batch(budget_bytes=200 * zones + (1 << 26), max_grids=len(sel) + 1,
+                   max_zones_per_grid=max(int(np.prod(s.full_shape[:3])) for s, _ in sel), device=device,
+                   **kw) as b:
+            for s, P in sel:
+                b.admit(s, P, 1e9)
+            b.step(3)
+            b.poll()
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            b.step(steps)
+            b.poll()
+            return (time.perf_counter() - t0) / steps
+
+    best = {}
+    sel1 = [(s, P) for s, P in grids if s.dims == 1]
+    timing1 = {c: time_batch(sel1, tile_1d=c, lockstep_1d=True) for c in (128, 256, 512)}
+    best["tile_1d"] = min(timing1, key=timing1.get)
+    best["timing_1d_ms"] = {str(k): v * 1e3 for k, v in timing1.items()}
+    sel2 = [(s, P) for s, P in grids if s.dims == 2]
+    cands = [("stage", t2, 0) for t2 in (1, 2, 3)] + [("persistent", t2, c) for t2 in (1, 2) for c in (2, 3, 4)]
+    timing = {}
+    for form, t2, ctas in cands:
+        timing[(form, t2, ctas)] = time_batch(sel2, tile_2d=t2, persistent=form == "persistent", ctas_per_sm=ctas)
+    form, t2, ctas = min(timing, key=timing.get)
+    best["tile_2d"] = t2
+    best["persistent"] = form == "persistent"
+    best["ctas_per_sm"] = ctas
+    best["timing_2d_ms"] = {f"{f}/{TILE_2D[t]}/{c}": v * 1e3 for (f, t, c), v in timing.items()}
+    if best["persistent"] and best["tile_1d"] not in (256, 512):
+        best["tile_1d"] = 256 if timing1[256] <= timing1[512] else 512
     os.makedirs(os.path.dirname(CACHE), exist_ok=True)
     with open(CACHE, "w") as f:
         json.dump(best, f, indent=1)

@@ -162,6 +162,127 @@ __global__ void k_batch_store(HGrid g, int buf, int g0, int g1, int N0, int N1, 
     for (int q = 0; q < 5; ++q) aos[c * 5 + q] = P[q];
 }
 
+// ---- the persistent step ----------------------------------------------------------
+// Every RK stage of every grid in the tile lists, for nsteps batch steps, in
+// one cooperative launch: the step start of every slot (k_batch_begin's
+// arithmetic), a grid-wide barrier, then per stage the CTAs stride over the
+// 1-D and the 2-D tiles together, a barrier after each stage.  CTAs read
+// what other CTAs of the launch wrote (stage outputs, dt, the buffer
+// rotation), so every such read goes to L2 (ld.global.cg); the arithmetic is
+// the tile kernels' (tile_stage), so a grid gives the same bits as with one
+// launch per stage.
+struct BatchArgs {
+    const HGrid* grids;
+    const TileRef* tiles1;
+    const TileRef* tiles2;
+    const int* ntiles;               // device-resident counts: [0] 1-D, [1] 2-D
+    int* rot;
+    double* t;
+    double* dt;
+    const double* tfin;
+    const double* cflp;
+    int* done;
+    int* pend;
+    long long* steps;
+    unsigned long long* cflbits;
+    unsigned* bar;                   // [0] arrivals, [1] generation
+    int* err;                        // set when a barrier wait gave up
+    int nslots, order, nsteps, flip;
+    float b[3];
+};
+
+constexpr int BATCH_POLLS = 1 << 24;  // a few seconds of waiting at a barrier, then an error
+
+// Grid-wide barrier of a cooperative launch (all CTAs resident): one thread
+// per CTA arrives on a counter; the last arrival resets it and bumps the
+// generation the others wait on.  Every wait is bounded: past the limit the
+// waiting CTA sets the error flag and returns false, as do CTAs that find the
+// flag set, so the launch ends and the host reads the error.
+__device__ __forceinline__ bool grid_barrier(const BatchArgs& A)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned* gen = A.bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(A.bar, 1u) == gridDim.x - 1) {
+            atomicExch(A.bar, 0u);
+            __threadfence();
+            atomicAdd(A.bar + 1, 1u);
+        } else {
+            int polls = 0;
+            while (*gen == g) {
+                if (*(volatile int*) A.err) { ok = 0; break; }
+                if (++polls > BATCH_POLLS) { atomicExch(A.err, 1); ok = 0; break; }
+                __nanosleep(polls < 64 ? 32 : 256);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// k_batch_begin for one slot, its operands read from L2
+__device__ __forceinline__ void batch_begin_slot(const BatchArgs& A, int s)
+{
+    if (__ldcg(A.done + s)) return;
+    if (__ldcg(A.pend + s)) {
+        A.t[s] = __ldcg(A.t + s) + __ldcg(A.dt + s);
+        A.steps[s] = __ldcg(A.steps + s) + 1;
+        if (A.flip) A.rot[s] = __ldcg(A.rot + s) ^ 1;
+        A.pend[s] = 0;
+    }
+    const double t = __ldcg(A.t + s), tf = __ldcg(A.tfin + s);
+    if (!(t < tf)) { A.done[s] = 2; return; }   // 2: finished (1: empty slot)
+    const double courant = __longlong_as_double((long long) __ldcg(A.cflbits + s));
+    double d = __ldcg(A.cflp + s) * courant;
+    const double d2 = tf - t;
+    A.dt[s] = d < d2 ? d : d2;
+    A.cflbits[s] = (unsigned long long) __double_as_longlong(DBL_MAX);
+    A.pend[s] = 1;
+}
+
+template <int RECON, int RIEMANN, int T1, int TY2>
+__global__ void __launch_bounds__(256, 4) batch_step_kernel(const __grid_constant__ BatchArgs A)
+{
+    __shared__ union {
+        TileSmem<1, RECON, T1, 1> s1;
+        TileSmem<2, RECON, 32, TY2> s2;
+    } sm;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    for (int step = 0; step < A.nsteps; ++step) {
+        for (int s = gtid; s < A.nslots; s += gstride) batch_begin_slot(A, s);
+        if (!grid_barrier(A)) return;
+        const int n1 = __ldcg(A.ntiles), n2 = __ldcg(A.ntiles + 1);
+        for (int rk = 0; rk < A.order; ++rk) {
+            const int last = rk == A.order - 1;
+            const float b = A.b[rk];
+            for (int w = blockIdx.x; w < n1 + n2; w += gridDim.x) {
+                const bool one = w < n1;
+                const TileRef tr = one ? A.tiles1[w] : A.tiles2[w - n1];
+                if (__ldcg(A.done + tr.grid)) continue;   // the same for the whole CTA
+                struct {
+                    const double* dtp;
+                    unsigned long long* slot;
+                    __device__ float dt() const { return (float) __ldcg(dtp); }
+                    __device__ unsigned long long* cfl() const { return slot; }
+                } at{A.dt + tr.grid, A.cflbits + tr.grid};
+                const int r = __ldcg(A.rot + tr.grid);
+                if (one)
+                    tile_stage<1, RECON, RIEMANN, T1, 1, 256, true>(sm.s1, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
+                                                                    last, at);
+                else
+                    tile_stage<2, RECON, RIEMANN, 32, TY2, 256, true>(sm.s2, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
+                                                                      last, at);
+            }
+            if (!grid_barrier(A)) return;
+        }
+    }
+}
+
 } // namespace mara
 
 using namespace mara;
@@ -216,6 +337,11 @@ struct MaraBatch {
     // one captured step per combination of non-empty tile lists (bit 0: 1-D,
     // bit 1: 2-D), so that a step launches only the lists that hold tiles
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    // the persistent form: one cooperative launch per mara_batch_step call
+    bool persistent = false;
+    int pgrid = 0;           // its CTAs (SMs x CTAs per SM)
+    unsigned* bar = nullptr; // grid barrier: arrivals, generation
+    int* kerr = nullptr;     // set by a barrier wait that gave up
 };
 
 typedef void (*TileKernel)(const HGrid*, const TileRef*, const int*, const int*, const double*, int, const int*, int,
@@ -287,6 +413,66 @@ static void enqueue_batch_step(MaraBatch* b, int mask)
                                         1.f - bb, last, b->cflbits, 1);
         }
     }
+}
+
+template <int RECON, int RIEMANN, int T1, int TY2>
+static const void* persistent_fn()
+{
+    return (const void*) batch_step_kernel<RECON, RIEMANN, T1, TY2>;
+}
+
+// the persistent kernel for the batch's scheme and tile shapes, or null when
+// the shapes have no persistent form (1-D tiles of 128 zones, 64 x 8 tiles)
+static const void* persistent_kernel(const MaraBatch* b)
+{
+    const bool plm = b->cfg.recon == MARA_RECON_PLM, hllc = b->cfg.riemann == MARA_RIEMANN_HLLC;
+    if ((b->tile1 != 256 && b->tile1 != 512) || (b->tile2 != 1 && b->tile2 != 2)) return nullptr;
+    const int k = (plm ? 8 : 0) + (hllc ? 4 : 0) + (b->tile1 == 512 ? 2 : 0) + (b->tile2 == 2 ? 1 : 0);
+    switch (k) {
+        case 0: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 8>();
+        case 1: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 16>();
+        case 2: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 8>();
+        case 3: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 16>();
+        case 4: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 8>();
+        case 5: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 16>();
+        case 6: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 8>();
+        case 7: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 16>();
+        case 8: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 8>();
+        case 9: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 16>();
+        case 10: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 8>();
+        case 11: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 16>();
+        case 12: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 8>();
+        case 13: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 16>();
+        case 14: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 8>();
+        default: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 16>();
+    }
+}
+
+static cudaError_t launch_persistent(MaraBatch* b, int nsteps)
+{
+    BatchArgs A;
+    A.grids = b->grids;
+    A.tiles1 = b->tiles[0];
+    A.tiles2 = b->tiles[1];
+    A.ntiles = b->ntiles;
+    A.rot = b->rot;
+    A.t = b->t;
+    A.dt = b->dt;
+    A.tfin = b->tfin;
+    A.cflp = b->cflp;
+    A.done = b->done;
+    A.pend = b->pend;
+    A.steps = b->steps;
+    A.cflbits = b->cflbits;
+    A.bar = b->bar;
+    A.err = b->kerr;
+    A.nslots = b->nslots;
+    A.order = b->cfg.rk_order;
+    A.nsteps = nsteps;
+    A.flip = b->cfg.rk_order == 1 ? 1 : 0;
+    for (int k = 0; k < 3; ++k) A.b[k] = B_TABLE[A.order - 1][k];
+    void* args[] = {(void*) &A};
+    return cudaLaunchCooperativeKernel(persistent_kernel(b), dim3(b->pgrid), dim3(256), args, 0, b->stream);
 }
 
 static int launches_per_step(const MaraBatch* b)
@@ -427,6 +613,8 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
     A((void**) &b->steps, sizeof(long long) * n);
     A((void**) &b->cflbits, sizeof(unsigned long long) * n);
     A((void**) &b->ntiles, sizeof(int) * 2);
+    A((void**) &b->bar, sizeof(unsigned) * 2);
+    A((void**) &b->kerr, sizeof(int));
     // tile capacity: the budget bounds the zones resident at once
     const int64_t max_zones = c->hbm_budget_bytes / 40 + 1;   // >= 2 buffers x 20 B per zone
     b->max_tiles[0] = (int) std::min<int64_t>(max_zones / 128 + n + 16, 1 << 26);
@@ -455,6 +643,8 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
         std::vector<int> ones(n, 1);
         cudaMemcpy(b->done, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
         cudaMemset(b->ntiles, 0, sizeof(int) * 2);
+        cudaMemset(b->bar, 0, sizeof(unsigned) * 2);
+        cudaMemset(b->kerr, 0, sizeof(int));
         cudaMemset(b->rot, 0, sizeof(int) * n);
         cudaMemset(b->pend, 0, sizeof(int) * n);
         for (int d = 0; d < 2; ++d) {
@@ -462,6 +652,20 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
             tile_dims(b, d + 1, &tx, &ty, &nt);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*) kernel_for(b, d + 1), nt, 0);
             b->ctas[d] = std::max(1, per) * b->sms;
+        }
+        // the persistent form: every CTA resident (a cooperative launch),
+        // ctas_per_sm of them per SM up to what the kernel's resources allow
+        const void* pk = c->persistent ? persistent_kernel(b) : nullptr;
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+        if (pk && coop) {
+            int per = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pk, 256, 0);
+            const int want = c->ctas_per_sm > 0 ? c->ctas_per_sm : per;
+            if (per > 0) {
+                b->persistent = true;
+                b->pgrid = std::min(want, per) * b->sms;
+            }
         }
         rc = cuda_rc(cudaDeviceSynchronize());
     }
@@ -484,6 +688,8 @@ int mara_batch_destroy(MaraBatch* b)
     if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->ev_main_end) cudaEventDestroy(b->ev_main_end);
     for (auto& g : b->graph) if (g) cudaGraphExecDestroy(g);
+    cudaFree(b->bar);
+    cudaFree(b->kerr);
     cudaFree(b->pend);
     for (auto& h : b->slots)
         for (int k = 0; k < 6; ++k)
@@ -579,7 +785,7 @@ int mara_batch_step(MaraBatch* b, int steps)
         b->launches += 2;
     }
     const int mask = list_mask(b);
-    if (!b->graph[mask]) {
+    if (!b->persistent && !b->graph[mask]) {
         cudaGraph_t g;
         BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         enqueue_batch_step(b, mask);
@@ -603,7 +809,15 @@ int mara_batch_step(MaraBatch* b, int steps)
             b->launches += 1;
         }
     }
-    for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph[mask], b->stream));
+    if (b->persistent && steps > 0) {
+        if (mask) {
+            BK(launch_persistent(b, steps));
+            b->launches += 1;
+        }
+    } else {
+        for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph[mask], b->stream));
+        b->launches += (int64_t) steps * launches_per_step(b);
+    }
     if (side && steps > 0) {
         BK(cudaEventRecord(b->ev_main_end, b->stream));
         for (int k = 0; k < CLUSTER_BUCKETS; ++k)
@@ -612,7 +826,6 @@ int mara_batch_step(MaraBatch* b, int steps)
         b->round_mask = mask;
     }
     b->step_count += steps;
-    b->launches += (int64_t) steps * launches_per_step(b);
     return MARA_OK;
 }
 
@@ -623,6 +836,11 @@ int mara_batch_poll(MaraBatch* b, int* slots, int cap, int* n)
     std::vector<int> d(b->nslots);
     BK(cudaMemcpyAsync(d.data(), b->done, sizeof(int) * b->nslots, cudaMemcpyDeviceToHost, b->stream));
     BK(cudaStreamSynchronize(b->stream));
+    if (b->persistent) {
+        int err = 0;
+        BK(cudaMemcpy(&err, b->kerr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return MARA_ERR_CUDA;   // a barrier wait gave up: the batch's state is not usable
+    }
     adapt_cluster_steps(b);
     int m = 0;
     for (int k = 0; k < b->nslots; ++k) {
@@ -700,3 +918,11 @@ int mara_batch_tiles(MaraBatch* b, int* t1, int* t2)
 }
 
 } // extern "C"
+
+int mara_batch_launch_form(MaraBatch* b, int* persistent, int* ctas)
+{
+    if (!b || !persistent || !ctas) return MARA_ERR_ARGUMENT;
+    *persistent = b->persistent ? 1 : 0;
+    *ctas = b->persistent ? b->pgrid : b->ctas[1];
+    return MARA_OK;
+}

@@ -167,3 +167,53 @@ def test_serving_loop_completes_and_matches_alone(gpu_lib):
         Pm, tm, nm = res.results[r.index]
         assert na == nm
         assert np.array_equal(Pa[s.interior()].view(np.uint64), Pm[s.interior()].view(np.uint64))
+
+
+PERSISTENT = [("plm", "hllc", 2, 512, 2), ("plm", "hlle", 3, 256, 1), ("pcm", "hllc", 1, 256, 2),
+              ("pcm", "hlle", 2, 512, 1)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("recon,riemann,rk,tile_1d,tile_2d", PERSISTENT)
+def test_persistent_launch_matches_per_stage_launches(gpu_lib, recon, riemann, rk, tile_1d, tile_2d):
+    """The persistent form (every stage of every step of a call in one
+    cooperative launch, grid-wide barriers between stages, stage inputs read
+    through L2) against one launch per stage and tile list: 1-D and 2-D
+    grids together in the tile lists, the same clock, step count and bits;
+    and CTAs per SM from 2 to the occupancy limit."""
+    from mara2_gb300.batch import Batch
+    reqs = W.riemann_stream(24, rate=1e6, seed=17, n1=(64, 2048), n2=(32, 160))
+    built = []
+    for r in reqs[:14]:
+        s, P = W.riemann_initial(r)
+        s = s.with_(recon=recon, riemann=riemann, rk_order=rk, t_final=0.01, guard=2)
+        built.append((s, W.apply_bc_numpy(s, P)))
+    kw = dict(recon=recon, riemann=riemann, rk_order=rk, tile_1d=tile_1d, tile_2d=tile_2d, lockstep_1d=True)
+    ref = _run_batch(built, **kw)
+    for ctas in (2, 0):
+        got = _run_batch(built, persistent=True, ctas_per_sm=ctas, **kw)
+        for k, (s, _) in enumerate(built):
+            Pa, ta, na = ref[k]
+            Pb, tb, nb = got[k]
+            assert na == nb and ta == tb, (k, na, nb)
+            assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), k
+    cells = max(int(np.prod(s.full_shape[:3])) for s, _ in built)
+    with Batch(budget_bytes=1 << 26, max_grids=4, max_zones_per_grid=cells, persistent=True, **kw) as b:
+        persistent, ctas = b.launch_form()
+        assert persistent and ctas > 0
+
+
+@pytest.mark.gpu
+def test_persistent_serving_alone_equals_mix(gpu_lib):
+    """Continuous batching on the persistent form: each request's result is
+    the same alone and in the mix (small 1-D grids on their clusters)."""
+    from mara2_gb300.batch import run_alone, serve
+    reqs = _small_requests(10, seed=41)
+    res = serve(reqs, budget_bytes=1 << 28, max_grids=32, keep_results=True, make=_make, persistent=True)
+    assert res.completed == len(reqs)
+    for r in reqs:
+        s, P = _make(r)
+        Pa, ta, na = run_alone(s, P, s.t_final)
+        Pm, tm, nm = res.results[r.index]
+        assert na == nm and ta == tm
+        assert np.array_equal(Pa[s.interior()].view(np.uint64), Pm[s.interior()].view(np.uint64))
