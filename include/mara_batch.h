@@ -4,10 +4,10 @@
  * 2-D) resident on one GPU, advanced together over a tile list that spans
  * all of them, each grid with its own dt = min(cfl * Courant, t_final - t)
  * (the reference's driver loop, src/Problems.cpp:181-188, per grid).  With
- * `persistent` set, every RK stage of every step of one mara_batch_step call
- * is one cooperative launch (grid-wide barriers between stages); otherwise
- * each stage is a launch per tile list and the step is captured once as a
- * CUDA graph.  Admitting and retiring grids edits device-resident tables
+ * `persistent` set, every RK stage of a batch step over both tile lists is
+ * one cooperative launch (grid-wide barriers between stages); otherwise each
+ * stage is a launch per tile list and the step is captured once as a CUDA
+ * graph.  Admitting and retiring grids edits device-resident tables
  * only.
  *
  * There is no counterpart of the batch in the reference (its drivers run
@@ -46,10 +46,10 @@ typedef struct MaraBatchConfig {
     int tile_2d;               /* 2-D tile: 0=auto, 1=32x8, 2=32x16, 3=64x8 */
     int lockstep_1d;           /* 1: small 1-D grids step with the tile lists
                                   (0: on thread-block clusters, see below)  */
-    int persistent;            /* 1: one cooperative launch per
-                                  mara_batch_step call (1-D tiles of 256 or
-                                  512 zones, 2-D tiles 32x8 or 32x16; other
-                                  shapes keep the per-stage launches)       */
+    int persistent;            /* 1: one cooperative launch per batch step
+                                  (1-D tiles of 256 or 512 zones, 2-D tiles
+                                  32x8 or 32x16; other shapes keep the
+                                  per-stage launches)                       */
     int ctas_per_sm;           /* CTAs per SM of that launch; 0 = as many as
                                   the kernel's resources allow              */
 } MaraBatchConfig;
@@ -101,7 +101,7 @@ int mara_batch_stats(MaraBatch* b, MaraBatchStats* stats);
 int mara_batch_tiles(MaraBatch* b, int* tile_1d, int* tile_2d);
 
 /* The launch form in use: *persistent = 1 with *ctas CTAs in the one
- * cooperative launch per call, or 0 with *ctas CTAs per 2-D stage launch.
+ * cooperative launch per step, or 0 with *ctas CTAs per 2-D stage launch.
  * No counterpart in the reference (it has no batch). */
 int mara_batch_launch_form(MaraBatch* b, int* persistent, int* ctas);
 

@@ -163,14 +163,19 @@ __global__ void k_batch_store(HGrid g, int buf, int g0, int g1, int N0, int N1, 
 }
 
 // ---- the persistent step ----------------------------------------------------------
-// Every RK stage of every grid in the tile lists, for nsteps batch steps, in
-// one cooperative launch: the step start of every slot (k_batch_begin's
+// Every RK stage of every grid in the tile lists for one batch step, in one
+// cooperative launch: the step start of every slot (k_batch_begin's
 // arithmetic), a grid-wide barrier, then per stage the CTAs stride over the
-// 1-D and the 2-D tiles together, a barrier after each stage.  CTAs read
-// what other CTAs of the launch wrote (stage outputs, dt, the buffer
-// rotation), so every such read goes to L2 (ld.global.cg); the arithmetic is
-// the tile kernels' (tile_stage), so a grid gives the same bits as with one
-// launch per stage.
+// 1-D and the 2-D tiles together (MASK: which lists the kernel serves), a
+// barrier between stages.  CTAs read what other CTAs of the launch wrote:
+// the per-slot scalars (dt, the buffer rotation, done) through L2
+// (ld.global.cg), and a stage's input, which the previous stage wrote, with
+// ordinary loads - no SM has read those lines earlier in the launch (stage
+// k reads rotation buffer k, which only stage k - 1 wrote, and U0, which no
+// stage before the last writes), so its L1 holds no stale copy, and the
+// kernel boundary orders one step's writes before the next step's reads.
+// The arithmetic is the tile kernels' (tile_stage), so a grid gives the same
+// bits as with one launch per stage.
 struct BatchArgs {
     const HGrid* grids;
     const TileRef* tiles1;
@@ -187,7 +192,7 @@ struct BatchArgs {
     unsigned long long* cflbits;
     unsigned* bar;                   // [0] arrivals, [1] generation
     int* err;                        // set when a barrier wait gave up
-    int nslots, order, nsteps, flip;
+    int nslots, order, flip;
     float b[3];
 };
 
@@ -245,7 +250,7 @@ __device__ __forceinline__ void batch_begin_slot(const BatchArgs& A, int s)
     A.pend[s] = 1;
 }
 
-template <int RECON, int RIEMANN, int T1, int TY2>
+template <int RECON, int RIEMANN, int T1, int TY2, int MASK>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel(const __grid_constant__ BatchArgs A)
 {
     __shared__ union {
@@ -253,33 +258,36 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel(const __grid_constan
         TileSmem<2, RECON, 32, TY2> s2;
     } sm;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    for (int step = 0; step < A.nsteps; ++step) {
-        for (int s = gtid; s < A.nslots; s += gstride) batch_begin_slot(A, s);
-        if (!grid_barrier(A)) return;
-        const int n1 = __ldcg(A.ntiles), n2 = __ldcg(A.ntiles + 1);
-        for (int rk = 0; rk < A.order; ++rk) {
-            const int last = rk == A.order - 1;
-            const float b = A.b[rk];
-            for (int w = blockIdx.x; w < n1 + n2; w += gridDim.x) {
-                const bool one = w < n1;
-                const TileRef tr = one ? A.tiles1[w] : A.tiles2[w - n1];
-                if (__ldcg(A.done + tr.grid)) continue;   // the same for the whole CTA
-                struct {
-                    const double* dtp;
-                    unsigned long long* slot;
-                    __device__ float dt() const { return (float) __ldcg(dtp); }
-                    __device__ unsigned long long* cfl() const { return slot; }
-                } at{A.dt + tr.grid, A.cflbits + tr.grid};
-                const int r = __ldcg(A.rot + tr.grid);
-                if (one)
-                    tile_stage<1, RECON, RIEMANN, T1, 1, 256, true>(sm.s1, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
-                                                                    last, at);
-                else
-                    tile_stage<2, RECON, RIEMANN, 32, TY2, 256, true>(sm.s2, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
-                                                                      last, at);
+    for (int s = gtid; s < A.nslots; s += gstride) batch_begin_slot(A, s);
+    if (!grid_barrier(A)) return;
+    const int n1 = MASK & 1 ? __ldcg(A.ntiles) : 0, n2 = MASK & 2 ? __ldcg(A.ntiles + 1) : 0;
+    for (int rk = 0; rk < A.order; ++rk) {
+        const int last = rk == A.order - 1;
+        const float b = A.b[rk];
+        for (int w = blockIdx.x; w < n1 + n2; w += gridDim.x) {
+            const bool one = w < n1;
+            const TileRef tr = one ? A.tiles1[w] : A.tiles2[w - n1];
+            if (__ldcg(A.done + tr.grid)) continue;   // the same for the whole CTA
+            struct {
+                const double* dtp;
+                unsigned long long* slot;
+                __device__ float dt() const { return (float) __ldcg(dtp); }
+                __device__ unsigned long long* cfl() const { return slot; }
+            } at{A.dt + tr.grid, A.cflbits + tr.grid};
+            const int r = __ldcg(A.rot + tr.grid);
+            if constexpr ((MASK & 1) != 0) {
+                if (one) {
+                    tile_stage<1, RECON, RIEMANN, T1, 1, 256, false>(sm.s1, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
+                                                                     last, at);
+                    continue;
+                }
             }
-            if (!grid_barrier(A)) return;
+            if constexpr ((MASK & 2) != 0)
+                tile_stage<2, RECON, RIEMANN, 32, TY2, 256, false>(sm.s2, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
+                                                                   last, at);
         }
+        // the last stage's Courant reductions are read by the next launch
+        if (!last && !grid_barrier(A)) return;
     }
 }
 
@@ -339,7 +347,7 @@ struct MaraBatch {
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     // the persistent form: one cooperative launch per mara_batch_step call
     bool persistent = false;
-    int pgrid = 0;           // its CTAs (SMs x CTAs per SM)
+    int pgrid[4] = {0, 0, 0, 0};  // its CTAs by tile-list mask (SMs x CTAs per SM)
     unsigned* bar = nullptr; // grid barrier: arrivals, generation
     int* kerr = nullptr;     // set by a barrier wait that gave up
 };
@@ -416,39 +424,43 @@ static void enqueue_batch_step(MaraBatch* b, int mask)
 }
 
 template <int RECON, int RIEMANN, int T1, int TY2>
-static const void* persistent_fn()
+static const void* persistent_fn(int mask)
 {
-    return (const void*) batch_step_kernel<RECON, RIEMANN, T1, TY2>;
+    // a kernel serving only one of the lists needs fewer registers
+    if (mask == 1) return (const void*) batch_step_kernel<RECON, RIEMANN, T1, 16, 1>;
+    if (mask == 2) return (const void*) batch_step_kernel<RECON, RIEMANN, 256, TY2, 2>;
+    return (const void*) batch_step_kernel<RECON, RIEMANN, T1, TY2, 3>;
 }
 
-// the persistent kernel for the batch's scheme and tile shapes, or null when
-// the shapes have no persistent form (1-D tiles of 128 zones, 64 x 8 tiles)
-static const void* persistent_kernel(const MaraBatch* b)
+// the persistent kernel for the batch's scheme, tile shapes and non-empty
+// tile lists (mask), or null when the shapes have no persistent form (1-D
+// tiles of 128 zones, 64 x 8 tiles)
+static const void* persistent_kernel(const MaraBatch* b, int mask)
 {
     const bool plm = b->cfg.recon == MARA_RECON_PLM, hllc = b->cfg.riemann == MARA_RIEMANN_HLLC;
     if ((b->tile1 != 256 && b->tile1 != 512) || (b->tile2 != 1 && b->tile2 != 2)) return nullptr;
     const int k = (plm ? 8 : 0) + (hllc ? 4 : 0) + (b->tile1 == 512 ? 2 : 0) + (b->tile2 == 2 ? 1 : 0);
     switch (k) {
-        case 0: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 8>();
-        case 1: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 16>();
-        case 2: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 8>();
-        case 3: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 16>();
-        case 4: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 8>();
-        case 5: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 16>();
-        case 6: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 8>();
-        case 7: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 16>();
-        case 8: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 8>();
-        case 9: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 16>();
-        case 10: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 8>();
-        case 11: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 16>();
-        case 12: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 8>();
-        case 13: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 16>();
-        case 14: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 8>();
-        default: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 16>();
+        case 0: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 8>(mask);
+        case 1: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 256, 16>(mask);
+        case 2: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 8>(mask);
+        case 3: return persistent_fn<RECON_PCM, RIEMANN_HLLE, 512, 16>(mask);
+        case 4: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 8>(mask);
+        case 5: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 256, 16>(mask);
+        case 6: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 8>(mask);
+        case 7: return persistent_fn<RECON_PCM, RIEMANN_HLLC, 512, 16>(mask);
+        case 8: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 8>(mask);
+        case 9: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 256, 16>(mask);
+        case 10: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 8>(mask);
+        case 11: return persistent_fn<RECON_PLM, RIEMANN_HLLE, 512, 16>(mask);
+        case 12: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 8>(mask);
+        case 13: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 256, 16>(mask);
+        case 14: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 8>(mask);
+        default: return persistent_fn<RECON_PLM, RIEMANN_HLLC, 512, 16>(mask);
     }
 }
 
-static cudaError_t launch_persistent(MaraBatch* b, int nsteps)
+static cudaError_t launch_persistent(MaraBatch* b, int mask)
 {
     BatchArgs A;
     A.grids = b->grids;
@@ -468,11 +480,11 @@ static cudaError_t launch_persistent(MaraBatch* b, int nsteps)
     A.err = b->kerr;
     A.nslots = b->nslots;
     A.order = b->cfg.rk_order;
-    A.nsteps = nsteps;
     A.flip = b->cfg.rk_order == 1 ? 1 : 0;
     for (int k = 0; k < 3; ++k) A.b[k] = B_TABLE[A.order - 1][k];
     void* args[] = {(void*) &A};
-    return cudaLaunchCooperativeKernel(persistent_kernel(b), dim3(b->pgrid), dim3(256), args, 0, b->stream);
+    return cudaLaunchCooperativeKernel(persistent_kernel(b, mask), dim3(b->pgrid[mask]), dim3(256), args, 0,
+                                       b->stream);
 }
 
 static int launches_per_step(const MaraBatch* b)
@@ -655,16 +667,16 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
         }
         // the persistent form: every CTA resident (a cooperative launch),
         // ctas_per_sm of them per SM up to what the kernel's resources allow
-        const void* pk = c->persistent ? persistent_kernel(b) : nullptr;
         int coop = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
-        if (pk && coop) {
-            int per = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pk, 256, 0);
-            const int want = c->ctas_per_sm > 0 ? c->ctas_per_sm : per;
-            if (per > 0) {
-                b->persistent = true;
-                b->pgrid = std::min(want, per) * b->sms;
+        if (c->persistent && coop && persistent_kernel(b, 3)) {
+            b->persistent = true;
+            for (int mask = 1; mask <= 3; ++mask) {
+                int per = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, persistent_kernel(b, mask), 256, 0);
+                const int want = c->ctas_per_sm > 0 ? c->ctas_per_sm : per;
+                b->pgrid[mask] = std::min(want, per) * b->sms;
+                if (per <= 0) b->persistent = false;
             }
         }
         rc = cuda_rc(cudaDeviceSynchronize());
@@ -811,8 +823,8 @@ int mara_batch_step(MaraBatch* b, int steps)
     }
     if (b->persistent && steps > 0) {
         if (mask) {
-            BK(launch_persistent(b, steps));
-            b->launches += 1;
+            for (int k = 0; k < steps; ++k) BK(launch_persistent(b, mask));
+            b->launches += steps;
         }
     } else {
         for (int k = 0; k < steps; ++k) BK(cudaGraphLaunch(b->graph[mask], b->stream));
@@ -923,6 +935,6 @@ int mara_batch_launch_form(MaraBatch* b, int* persistent, int* ctas)
 {
     if (!b || !persistent || !ctas) return MARA_ERR_ARGUMENT;
     *persistent = b->persistent ? 1 : 0;
-    *ctas = b->persistent ? b->pgrid : b->ctas[1];
+    *ctas = b->persistent ? b->pgrid[3] : b->ctas[1];
     return MARA_OK;
 }
