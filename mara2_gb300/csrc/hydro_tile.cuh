@@ -480,7 +480,9 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                 reinterpret_cast<double*>(Unh)[q * sU + o] = Un;
                 Unew[q] = __double2float_rn(Un);
             } else {
-                const df U0 = {ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
+                // U0 enters only with b < 1 (stage 1 is U + dt L)
+                const df U0 = b == 1.0f ? df{0.0f, 0.0f}
+                                        : df{ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
                 const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
                 const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
                 Unh[q * sU + o] = Un.hi;
