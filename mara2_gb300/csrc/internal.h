@@ -40,6 +40,11 @@ struct DevStatus {
     double t;                       // driver-loop time
     double dt;                      // dt of the current step
     long long steps;                // driver-loop steps taken
+    long long taken;                // steps that ran since the host last read the
+                                    // status: a step enqueued after t_final (or an
+                                    // error) does no work, so the ping-pong parity
+                                    // of the state follows this count, not the
+                                    // number of steps the host enqueued
     int halt;                       // a previous stage had inversion failures: the
                                     // step stops there, as the reference's
                                     // InversionFailure ends MethodOfLinesTVD::advance

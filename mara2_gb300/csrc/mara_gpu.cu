@@ -42,13 +42,26 @@ __global__ void k_dt_from_courant(DevStatus* st, double cfl, double t_final)
     st->dt = dt;
 }
 
-__global__ void k_set_dt(DevStatus* st, double dt) { st->dt = dt; }
+// an advance with a given dt is always taken (SolutionScheme::advance), also
+// after a driver loop stopped at t_final
+__global__ void k_set_dt(DevStatus* st, double dt)
+{
+    st->dt = dt;
+    st->done = 0;
+}
+
+// an advance that ran counts toward the state's ping-pong parity
+__global__ void k_step_taken(DevStatus* st)
+{
+    if (!st->done && !st->code && !st->halt) st->taken += 1;
+}
 
 __global__ void k_advance_time(DevStatus* st)
 {
     if (st->done || st->code) return;
     st->t += st->dt;
     st->steps += 1;
+    st->taken += 1;
 }
 
 __global__ void k_status_reset(DevStatus* st)
@@ -296,7 +309,9 @@ struct MaraGpuHandle {
     cudaStream_t aux = nullptr;          // host <-> device copies, overlapped with conversions
     cudaEvent_t ev[17] = {};             // per-chunk events, [16] joins the streams
     double* P[2] = {nullptr, nullptr};  // primitive state with guards (plain path)
-    int cur = 0;
+    int cur = 0;                         // P[cur] holds the state once the enqueued steps run
+    int cur_base = 0;                    // the parity when the device's count of steps
+                                         // taken was last reset
     double* U0 = nullptr;
     double* U = nullptr;
     double* F[3] = {nullptr, nullptr, nullptr};
@@ -508,15 +523,44 @@ static void enqueue_courant(MaraGpuHandle* h)
     h->launches += 2;
 }
 
+// With the stream idle: the state's buffer parity from the steps that ran
+// (the host flips its parity for every step it enqueues, also for steps that
+// find the loop done and do no work), and the count reset.
+static int settle_parity(MaraGpuHandle* h)
+{
+    const long long taken = h->st_host->taken;
+    if (h->mixed) {
+        mixed_sync_rotation(h->mixed, h->stream);
+    } else {
+        h->cur = (h->cur_base + (int) ((taken & 1) * (h->cfg.rk_order & 1))) & 1;
+        h->cur_base = h->cur;
+    }
+    if (taken) {
+        h->st_host->taken = 0;
+        CK(cudaMemsetAsync(&h->st->taken, 0, sizeof(long long), h->stream));
+    }
+    return MARA_OK;
+}
+
 static int read_status(MaraGpuHandle* h)
 {
     CK(cudaMemcpyAsync(h->st_host, h->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (const int rs_ = settle_parity(h)) return rs_;
     const DevStatus& s = *h->st_host;
     int status = s.code;
     if (status == 0 && s.failures > 0) status = MARA_ERR_INVERSION_FAILURE;
     h->last_status = status;
     return status;
+}
+
+// Wait for the enqueued work and settle the state's buffer before reading it
+// (download, diagnostics, Courant step): a status error is not a failure here.
+static int sync_state(MaraGpuHandle* h)
+{
+    CK(cudaMemcpyAsync(h->st_host, h->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return settle_parity(h);
 }
 
 static int clear_status(MaraGpuHandle* h)
@@ -662,6 +706,7 @@ int mara_gpu_upload(MaraGpuHandle* h, const double* P_aos)
     // are reported until then)
     k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
     h->launches++;
+    h->cur_base = h->cur;   // the new state is written into P[cur]; the count of steps taken restarts
     if (h->mixed) mixed_load_begin(h->mixed, h->stream);
     if (const double* d = (const double*) direct_host_pointer(P_aos)) {
         const long long cells = h->G.sP;
@@ -704,6 +749,7 @@ int mara_gpu_generate(MaraGpuHandle* h, const MaraInitialData* d)
     const long long total = h->G.sP;
     k_generate<<<(unsigned) ((total + 255) / 256), 256, 0, h->stream>>>(h->stage_aos, h->G, geo, *d);
     k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+    h->cur_base = h->cur;
     h->launches += 2;
     if (h->mixed) {
         mixed_load_begin(h->mixed, h->stream);
@@ -721,6 +767,7 @@ int mara_gpu_assign_vector_potential(MaraGpuHandle* h, const double* A, double s
     if (!h || !A) return MARA_ERR_ARGUMENT;
     if (h->cfg.law != MARA_LAW_MHD && h->cfg.law != MARA_LAW_RMHD) return MARA_ERR_CONFIG;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     const VecPot shape{nullptr, h->G.N[0] + 1, h->G.N[1] + 1, h->G.N[2] + 1};
     const size_t abytes = sizeof(double) * 9 * (size_t) shape.f0 * shape.f1 * shape.f2;
     double* dA = nullptr;
@@ -736,6 +783,7 @@ int mara_gpu_assign_vector_potential(MaraGpuHandle* h, const double* A, double s
         V.A = dA;
         k_assign_b<<<(unsigned) ((total + 255) / 256), 256, 0, h->stream>>>(h->stage_aos, h->G, V, scale);
         k_status_reset<<<1, 1, 0, h->stream>>>(h->st);
+        h->cur_base = h->cur;
         if (h->mixed) {
             mixed_load_begin(h->mixed, h->stream);
             mixed_load_aos_range(h->mixed, h->stage_aos, 0, total, h->st, h->stream);
@@ -755,6 +803,7 @@ int mara_gpu_download(MaraGpuHandle* h, double* P_aos)
 {
     if (!h || !P_aos) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     if (double* d = (double*) direct_host_pointer(P_aos)) {
         const long long cells = h->G.sP;
         if (h->mixed) mixed_store_aos_range(h->mixed, d, 0, cells, h->stream);
@@ -794,6 +843,8 @@ int mara_gpu_advance(MaraGpuHandle* h, double t0, double dt)
         h->launches++;
         enqueue_step(h);
         if (const int se = take_source_error(h)) return se;
+        k_step_taken<<<1, 1, 0, h->stream>>>(h->st);
+        h->launches++;
     }
     h->steps++;
     return cuda_status(cudaGetLastError());
@@ -827,6 +878,7 @@ int mara_gpu_courant(MaraGpuHandle* h, double* dt)
 {
     if (!h || !dt) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     enqueue_courant(h);
     const int rc = read_status(h);
     *dt = __builtin_bit_cast(double, h->st_host->dt_bits);
@@ -1024,6 +1076,7 @@ int mara_gpu_monopole(MaraGpuHandle* h, double mesh_spacing, double* max_abs)
     if (!h || !max_abs || !(mesh_spacing > 0.0)) return MARA_ERR_ARGUMENT;
     if (h->cfg.law == MARA_LAW_HYDRO) return MARA_ERR_CONFIG;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     const void* P = h->mixed ? (const void*) mixed_primitives(h->mixed) : (const void*) h->P[h->cur];
     if (!P) return MARA_ERR_CONFIG;
     unsigned long long* out = &h->st->dt_bits;  // scratch word: the next Courant call re-initialises it
@@ -1065,6 +1118,7 @@ int mara_gpu_volume_diagnostics(MaraGpuHandle* h, double* D, int* count)
 {
     if (!h || !D) return MARA_ERR_ARGUMENT;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     const size_t nd = DIAG_MAX;
     const size_t doubles = (size_t) DIAG_BLOCKS * nd + nd + 1;  // partials, totals, error word
     if (!h->diag) {
@@ -1094,6 +1148,7 @@ int mara_gpu_field_diagnostics(MaraGpuHandle* h, double mesh_spacing, double* ou
     if (!h || !out_aos || !(mesh_spacing > 0.0)) return MARA_ERR_ARGUMENT;
     if (h->cfg.law == MARA_LAW_HYDRO) return MARA_ERR_CONFIG;
     CK(cudaSetDevice(h->cfg.device));
+    if (const int rs_ = sync_state(h)) return rs_;
     const void* P = h->mixed ? (const void*) mixed_primitives(h->mixed) : (const void*) h->P[h->cur];
     if (!P) return MARA_ERR_CONFIG;
     const size_t bytes = (size_t) h->G.N[0] * h->G.N[1] * h->G.N[2] * 4 * sizeof(double);

@@ -730,7 +730,12 @@ __global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, cons
 
 __global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long long) __double_as_longlong(DBL_MAX); }
 __global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
-__global__ void k_rot_flip(int* rot) { *rot ^= 1; }
+// RK1 on the fused path alternates the state buffer; a step that found the
+// loop done (or an error) did no work and keeps it
+__global__ void k_rot_flip(int* rot, const DevStatus* st)
+{
+    if (!st->done && !st->code) *rot ^= 1;
+}
 // the general form's last stage reduced the new state's Courant step into
 // next; it becomes the handle's only if the step ran (a step not taken, at
 // t_final or after an error, leaves the previous state's step)
@@ -765,6 +770,7 @@ __global__ void k_fused_run_begin(unsigned long long* bits, DevStatus* st, doubl
 // Start of one advance with a given dt on the fused path.
 __global__ void k_fused_advance_begin(unsigned long long* bits, DevStatus* st, double dt)
 {
+    st->done = 0;   // an advance with a given dt is always taken
     st->dt = dt;
     *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
 }
@@ -1209,7 +1215,7 @@ static void fused_step(MixedState* m, const double* dt, DevStatus* st, cudaStrea
             else tile_dispatch<1>(m, dt, st, s, rk, b, last);
         });
     }
-    if (order == 1) k_rot_flip<<<1, 1, 0, s>>>(m->drot);
+    if (order == 1) k_rot_flip<<<1, 1, 0, s>>>(m->drot, st);
 }
 
 void mixed_enqueue_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int64_t*)
@@ -1751,6 +1757,13 @@ int mixed_enqueue_cluster_steps(MixedState* m, int nsteps, double cfl, double t_
                 : cluster_launch<RECON_PLM, RIEMANN_HLLE>(m, nsteps, cfl, t_final, st, s);
 }
 void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
+// the state buffer the device rotation holds (the stream is idle): steps
+// enqueued after the loop was done did not turn it
+void mixed_sync_rotation(MixedState* m, cudaStream_t s)
+{
+    cudaMemcpyAsync(&m->rot, m->drot, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+}
 void mixed_advance_parity(MixedState* m) { if (m->fused && m->cfg.rk_order == 1) m->rot ^= 1; }
 void mixed_set_timing(MixedState* m, int on) { m->timing = on; }
 const float* mixed_primitives(const MixedState* m) { return m->Pf; }

@@ -25,6 +25,7 @@ void mixed_enqueue_courant(MixedState* m, DevStatus* st, cudaStream_t s);
 // enqueued) otherwise.
 bool mixed_enqueue_run_step(MixedState* m, double cfl, double t_final, DevStatus* st, cudaStream_t s);
 bool mixed_enqueue_advance(MixedState* m, double dt, DevStatus* st, cudaStream_t s);
+void mixed_sync_rotation(MixedState* m, cudaStream_t s);
 // one advance of a page-locked host MeshData::P in place (host_dev: its
 // device address), the transfers and the stages pipelined in one launch
 // (2-D fused grids)
