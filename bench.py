@@ -425,7 +425,8 @@ def run_timed(s, P0, precision, device, t_final=None, steps=None):
     """Zone-updates/s of a device-driven run (dt on the device; with an end
     time the host looks at the device's done flag every 64 steps): CUDA
     events on the handle's stream around the run, after one untimed step
-    that computes the first Courant step."""
+    that computes the first Courant step (a run of a stated step count takes
+    that many steps in all)."""
     import torch
     from mara2_gb300.solver import Solver
     with Solver(s, precision, device) as g:
@@ -434,7 +435,7 @@ def run_timed(s, P0, precision, device, t_final=None, steps=None):
         g.run(1, s.cfl, t_final)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        n = g.run(steps if steps is not None else 10_000_000, s.cfl, t_final)
+        n = g.run(steps - 1 if steps is not None else 10_000_000, s.cfl, t_final)
         b.record(stream)
         b.synchronize()
         ms = a.elapsed_time(b)

@@ -4,11 +4,11 @@
  * 2-D) resident on one GPU, advanced together over a tile list that spans
  * all of them, each grid with its own dt = min(cfl * Courant, t_final - t)
  * (the reference's driver loop, src/Problems.cpp:181-188, per grid).  With
- * `persistent` set, every RK stage of a batch step over both tile lists is
- * one cooperative launch (grid-wide barriers between stages); otherwise each
- * stage is a launch per tile list and the step is captured once as a CUDA
- * graph.  Admitting and retiring grids edits device-resident tables
- * only.
+ * `persistent` set, a batch step (every RK stage over both tile lists) is
+ * one cooperative launch with grid-wide barriers between the stages;
+ * otherwise each stage is a launch per tile list and the step is captured
+ * once as a CUDA graph.  Both forms give the same bits.  Admitting and
+ * retiring grids edits device-resident tables only.
  *
  * There is no counterpart of the batch in the reference (its drivers run
  * one MeshData at a time); each grid's arithmetic is the mixed-precision

@@ -1,14 +1,16 @@
 """Batched grids and the serving loop over include/mara_batch.h.
 
-``Batch``  -- many resident hydro grids advanced together by one persistent
-             kernel per RK stage (the step replayed from a CUDA graph).
+``Batch``  -- many resident hydro grids advanced together: a launch per
+             tile list and RK stage (the step replayed from a CUDA graph),
+             or the whole step in one cooperative launch (``persistent``).
 ``serve``  -- continuous batching of a stream of requests: each request is
              admitted as soon as it has arrived and the HBM budget / grid
              table has room, advanced together with whatever else is
              resident, and retired (result copied to the host) as soon as it
              reaches its end time; reports throughput and p50/p99 latency.
-``autotune`` -- picks the 1-D and 2-D tile shapes by timing each candidate on
-             a representative mix, and caches the choice.
+``autotune`` -- picks the 1-D and 2-D tile shapes and the launch form (and
+             its CTAs per SM) by timing each candidate on a representative
+             mix, and caches the choice.
 """
 from __future__ import annotations
 

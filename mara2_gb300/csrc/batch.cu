@@ -4,12 +4,16 @@
 // Device tables, one entry per slot: HGrid (state pointers, shape, bc,
 // gamma), the driver state (t, dt, t_final, cfl factor, done, steps, Courant
 // bits) and the buffer rotation.  Two tile lists (1-D tiles, 2-D tiles) cover
-// every resident grid; each RK stage is two persistent launches of the fused
-// stage kernel (hydro_tile.cuh), one per list, whatever mix of grids is
-// resident.  A batch step -- per-grid dt, the RK stages, the per-grid Courant
-// reduction fused into the last stage, the time update -- is captured once
-// as a CUDA graph: admitting or retiring a grid rewrites the tables and the
-// tile lists (device-resident counts), never the graph.
+// every resident grid.  Two launch forms, with the same arithmetic and bits:
+// (stage form) each RK stage is two launches of the fused stage kernel
+// (hydro_tile.cuh), one per list, whose CTAs stride over the list whatever
+// mix of grids is resident, and a batch step -- per-grid dt, the RK stages,
+// the per-grid Courant reduction fused into the last stage, the time update
+// -- is captured once as a CUDA graph; (persistent form) every stage of a
+// batch step over both lists in one cooperative launch with grid-wide
+// barriers between the stages (batch_step_kernel).  Admitting or retiring a
+// grid rewrites the tables and the tile lists (device-resident counts),
+// never the graph or the launch.
 //
 // Memory: each grid holds its FP32-pair state (2 rotation buffers for RK1/2,
 // 3 for RK3) allocated stream-ordered from the device's memory pool and
