@@ -86,6 +86,8 @@ __device__ __forceinline__ void hydro_u2p_d(const double* U, double gm1, double*
 
 template <int RECON> struct HaloOf { static constexpr int G = RECON == RECON_PCM ? 1 : 2; };
 
+
+
 // ---- the FP32 arithmetic of the fused kernels --------------------------------
 // Every operation is an explicitly rounded intrinsic or a PTX approximate
 // reciprocal / square root, so that no multiply and add are fused differently
@@ -266,6 +268,7 @@ template <int DIM, int RECON, int TX, int TY>
 struct TileSmem {
     static constexpr int G = HaloOf<RECON>::G;
     float Ps[5][DIM == 2 ? TY + 2 * G : 1][TX + 2 * G];
+    float Uc[5][TY][TX];   // the stage input's high words of the tile's zones
     float Fx[5][TY][TX + 1];
     float Fy[5][DIM == 2 ? TY + 1 : 1][DIM == 2 ? TX : 1];
 };
@@ -318,7 +321,8 @@ __device__ __forceinline__ double rk_combine_d(double U0, double U, float dtL, f
 //   tile's Courant step goes to *at.cfl().  at.dt() and at.cfl() are read
 //   where they are used, so that neither holds registers across the tile.
 //   ACC64: the state arrays (Uh) hold the FP64 accumulator, Ul is unused.
-template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, class At>
+template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, bool EARLY = false,
+          class At>
 __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, const HGrid& g, const TileRef& tr,
                                            int s, int stage, float b, float omb, int last, const At& at)
 {
@@ -404,6 +408,15 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                 const int lx = c % WX, ly = c / WX;
                 if (fl[k] & 1) Ur[k][1] = -Ur[k][1];
                 if (fl[k] & 2) Ur[k][2] = -Ur[k][2];
+                if constexpr (EARLY && !ACC64) {
+                    // a zone of the tile itself: keep its conserved high words
+                    // for the update (halo zones of a tile never are)
+                    const int zx = lx - G, zy = DIM == 2 ? ly - G : 0;
+                    if (zx >= 0 && zx < TX && zy >= 0 && zy < TY) {
+#pragma unroll
+                        for (int q = 0; q < 5; ++q) sm.Uc[q][zy][zx] = Ur[k][q];
+                    }
+                }
                 float P[5];
                 fh_cons(g.gamma, Ur[k], P);
 #pragma unroll
@@ -446,11 +459,8 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
             for (int q = 0; q < 5; ++q) sm.Fy[q][fy][fx] = Fh[q];
         }
     }
-    __syncthreads();
 
     // 3. divergence, RK combine, store
-    const float dt = at.dt();
-    float zdt = 3.0e38f;
     // the rotation's three buffers are distinct arrays
     const float* __restrict__ U0h = g.Uh[s];
     const float* __restrict__ U0l = g.Ul[s];
@@ -459,45 +469,109 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     float* __restrict__ Unh = g.Uh[dst];
     float* __restrict__ Unl = g.Ul[dst];
     const float idx = g.idx, idy = g.idy;
-    for (int c = threadIdx.x; c < TX * TY; c += NT) {
-        const int lx = c % TX, ly = c / TX;
-        const int x = tr.x0 + lx, y = tr.y0 + ly;
-        if (x >= n0 || y >= n1) continue;
-        const long long o = (long long) y * n0 + x;
-        float Unew[5];
+    float zdt = 3.0e38f;
+    if constexpr (EARLY && !ACC64) {
+        // Each thread's zones' operands from HBM (the stage input's low
+        // words and, after the first stage, both words of U0; the high words
+        // of the stage input were kept in shared memory when the tile was
+        // staged) are loaded before the barrier that ends the face phase, so
+        // that their latency overlaps the wait for the other threads' faces.
+        // Nothing in this launch writes them before this CTA's own stores.
+        constexpr int NZ = (TX * TY + NT - 1) / NT;
+        float r_pl[NZ][5], r_0h[NZ][5], r_0l[NZ][5];
+        auto load = [&](int z) {
+            const int c = threadIdx.x + z * NT;
+            const int x = tr.x0 + c % TX, y = tr.y0 + c / TX;
+            if (c < TX * TY && x < n0 && y < n1) {
+                const long long o = (long long) y * n0 + x;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            float L;
-            if constexpr (DIM == 2)
-                L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx, sm.Fy[q][ly][lx], sm.Fy[q][ly + 1][lx], idy);
-            else
-                L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx);
-            if constexpr (ACC64) {
-                const double* U0d = reinterpret_cast<const double*>(U0h) + q * sU + o;
-                const double* Upd = reinterpret_cast<const double*>(Uph) + q * sU + o;
-                const double u0 = b == 1.0f ? 0.0 : (L2ONLY ? __ldcg(U0d) : *U0d);
-                const double Un = rk_combine_d(u0, L2ONLY ? __ldcg(Upd) : *Upd, f_mul(dt, L), b);
-                reinterpret_cast<double*>(Unh)[q * sU + o] = Un;
-                Unew[q] = __double2float_rn(Un);
-            } else {
-                // U0 enters only with b < 1 (stage 1 is U + dt L)
-                const df U0 = b == 1.0f ? df{0.0f, 0.0f}
-                                        : df{ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
-                const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
-                const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
+                for (int q = 0; q < 5; ++q) {
+                    r_pl[z][q] = ld_state<L2ONLY>(Upl + q * sU + o);
+                    // U0 enters only with b < 1 (stage 1 is U + dt L)
+                    r_0h[z][q] = b == 1.0f ? 0.0f : ld_state<L2ONLY>(U0h + q * sU + o);
+                    r_0l[z][q] = b == 1.0f ? 0.0f : ld_state<L2ONLY>(U0l + q * sU + o);
+                }
+            }
+        };
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) load(z);
+        __syncthreads();
+        const float dt = at.dt();
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) {
+            const int c = threadIdx.x + z * NT;
+            const int lx = c % TX, ly = c / TX;
+            const int x = tr.x0 + lx, y = tr.y0 + ly;
+            if (c >= TX * TY || x >= n0 || y >= n1) continue;
+            const long long o = (long long) y * n0 + x;
+            float Unew[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                float L;
+                if constexpr (DIM == 2)
+                    L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx, sm.Fy[q][ly][lx], sm.Fy[q][ly + 1][lx], idy);
+                else
+                    L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx);
+                const df Un = rk_combine(df{r_0h[z][q], r_0l[z][q]}, df{sm.Uc[q][ly][lx], r_pl[z][q]}, f_mul(dt, L), b, omb);
                 Unh[q * sU + o] = Un.hi;
                 Unl[q * sU + o] = Un.lo;
                 Unew[q] = Un.hi;
             }
+            if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
         }
-        if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
+    } else {
+        // operands loaded zone by zone after the barrier (the kernels that
+        // run a tile stage inside a larger loop keep to 64 registers)
+        __syncthreads();
+        const float dt = at.dt();
+        for (int c = threadIdx.x; c < TX * TY; c += NT) {
+            const int lx = c % TX, ly = c / TX;
+            const int x = tr.x0 + lx, y = tr.y0 + ly;
+            if (x >= n0 || y >= n1) continue;
+            const long long o = (long long) y * n0 + x;
+            float Unew[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                float L;
+                if constexpr (DIM == 2)
+                    L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx, sm.Fy[q][ly][lx], sm.Fy[q][ly + 1][lx], idy);
+                else
+                    L = fh_div(sm.Fx[q][ly][lx], sm.Fx[q][ly][lx + 1], idx);
+                if constexpr (ACC64) {
+                    const double* U0d = reinterpret_cast<const double*>(U0h) + q * sU + o;
+                    const double* Upd = reinterpret_cast<const double*>(Uph) + q * sU + o;
+                    const double u0 = b == 1.0f ? 0.0 : (L2ONLY ? __ldcg(U0d) : *U0d);
+                    const double Un = rk_combine_d(u0, L2ONLY ? __ldcg(Upd) : *Upd, f_mul(dt, L), b);
+                    reinterpret_cast<double*>(Unh)[q * sU + o] = Un;
+                    Unew[q] = __double2float_rn(Un);
+                } else {
+                    // U0 enters only with b < 1 (stage 1 is U + dt L)
+                    const df U0 = b == 1.0f ? df{0.0f, 0.0f}
+                                            : df{ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
+                    const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
+                    const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
+                    Unh[q * sU + o] = Un.hi;
+                    Unl[q * sU + o] = Un.lo;
+                    Unew[q] = Un.hi;
+                }
+            }
+            if (last) zdt = fminf(zdt, hydro_zone_dt(g, Unew));
+        }
     }
     if (last) block_min_to(at.cfl(), zdt);
 }
 
+// Resident CTAs per SM the stage kernels are compiled for: the FP32-pair
+// update holds its zones' operands across the face phase's barrier, which
+// wants up to 85 registers a thread (3 CTAs of 256 threads per SM: 3 % faster
+// on KH 1024^2 than 4 CTAs at 64 registers with spills, or than the operands
+// loaded after the barrier); the FP64-accumulator form stays at 64 registers
+// and 4 CTAs.
+template <int NT, bool ACC64> struct TileOccupancy { static constexpr int CTAS = ACC64 ? 1024 / NT : 768 / NT; };
+
 // One RK stage over a list of tiles (persistent: CTAs stride over tiles).
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool ACC64 = false>
-__global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict__ grids,
+__global__ void __launch_bounds__(NT, (TileOccupancy<NT, ACC64>::CTAS)) hydro_tile_kernel(const HGrid* __restrict__ grids,
                                                         const TileRef* __restrict__ tiles,
                                                         const int* __restrict__ ntiles_p,
                                                         const int* __restrict__ rot,  // per grid: state buffer s
@@ -518,7 +592,7 @@ __global__ void __launch_bounds__(NT) hydro_tile_kernel(const HGrid* __restrict_
             __device__ float dt() const { return (float) *dtp; }
             __device__ unsigned long long* cfl() const { return slot; }
         } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride};
-        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
+        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64, true>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
     }
 }
 
