@@ -583,6 +583,100 @@ def workload_suite(device: int, serving_requests: int = 4096):
     return out
 
 
+def _events_ms(solver, device, fn, reps: int) -> float:
+    """Mean device ms of fn() (work enqueued on the handle's stream), CUDA
+    events on that stream around each call, one untimed call first."""
+    import torch
+    stream = torch.cuda.ExternalStream(solver.stream, device=torch.device("cuda", device))
+    fn()
+    ms = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    return float(np.mean(ms))
+
+
+def next_rows_suite(device: int, peak_hbm: float):
+    """The rows beside the time step (device diagnostics, device initial
+    data, source terms) measured on the resident state: device ms per call
+    (CUDA events on the handle's stream; each call also returns its result to
+    the host), the algorithmic bytes each call must move in HBM and the
+    achieved fraction of the measured HBM rate."""
+    from mara2_gb300 import workloads as W
+    from mara2_gb300.solver import Solver
+    out = {}
+
+    def hbm(ms, nbytes):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return {"ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak_hbm}
+
+    # FieldOperator::volumeIntegratedDiagnostics and the largest
+    # CellCenteredFieldCT::monopole on MHD 256^3: each reads the resident
+    # state once (8 fields; the field's 3 for the monopole) at 8 B a value
+    s, P0 = W.mhd_turbulence(256)
+    for prec in ("fp64", "mixed"):
+        with Solver(s, prec, device) as g:
+            g.upload(P0)
+            ms = _events_ms(g, device, g.volume_diagnostics, 10)
+            out[f"volume_diagnostics_mhd256_{prec}"] = hbm(ms, s.zones * 8 * 8)
+            ms = _events_ms(g, device, lambda: g.monopole_max(1.0 / 256), 10)
+            out[f"monopole_max_mhd256_{prec}"] = hbm(ms, s.zones * 3 * 8)
+    # the checkpoint's cell fields (monopole, current) to the host: 4 doubles a
+    # cell with guards over the host link, into page-locked and into pageable
+    # host memory
+    import torch
+    with Solver(s, "fp64", device) as g:
+        g.upload(P0)
+        cells = int(np.prod(s.full_shape[:3]))
+        pinned = torch.empty(tuple(s.full_shape[:3]) + (4,), dtype=torch.float64).pin_memory().numpy()
+        for name, buf in (("page_locked", pinned), ("pageable", None)):
+            ms = _events_ms(g, device, lambda: g.field_diagnostics(1.0 / 256, buf), 3)
+            out[f"field_diagnostics_mhd256_to_host_{name}"] = {"ms": ms, "bytes_to_host": cells * 32,
+                                                               "achieved_gbs": cells * 32 / (ms * 1e-3) / 1e9}
+        del pinned
+    del P0
+
+    # MeshOperator::generate on the device: the KH shear layer with its
+    # seeded perturbation written into the resident state (FP64 primitives
+    # with guards; FP32 pairs of conserved densities)
+    s, spec = W.device_initial_data("kh", 1024)
+    for prec in ("fp64", "mixed"):
+        with Solver(s, prec, device) as g:
+            ms = _events_ms(g, device, lambda: g.generate(spec), 10)
+            nbytes = int(np.prod(s.full_shape[:3])) * 5 * 8 if prec == "fp64" else s.zones * 5 * 8
+            out[f"generate_kh1024_{prec}"] = hbm(ms, nbytes)
+
+    # source terms (SolutionSchemes.cpp:219-228): the plain step of KH 1024^2
+    # with the library's uniform gravity against the same step without
+    s, P0 = W.kelvin_helmholtz(1024)
+    with Solver(s, "fp64", device) as g:
+        g.upload(P0)
+        dt = 0.2 * g.courant()
+        base = _events_ms(g, device, lambda: g.advance(dt), 5)
+        g.set_source_terms(gravity=(0.0, -0.1, 0.0))
+        with_src = _events_ms(g, device, lambda: g.advance(dt), 5)
+        g.set_source_terms()
+        out["source_terms_gravity_kh1024_fp64"] = {"step_ms": base, "step_ms_with_source": with_src,
+                                                   "overhead": with_src / base - 1.0}
+    # NewtonianMHD cooling (an auxiliary field, ConservationLaws.cpp:489-501)
+    # on the plain MHD 128^3 step against the same step without
+    s, P0 = W.mhd_turbulence(128)
+    sc, P1 = W.with_cooling(s, P0.copy(), 0.4, aux=0.02)
+    steps = {}
+    for name, ss, PP in (("base", s, P0), ("cooling", sc, P1)):
+        with Solver(ss, "fp64", device) as g:
+            g.upload(PP)
+            dt = 0.2 * g.courant()
+            steps[name] = _events_ms(g, device, lambda: g.advance(dt), 3)
+    out["source_terms_cooling_mhd128_fp64"] = {"step_ms": steps["base"], "step_ms_with_cooling": steps["cooling"],
+                                               "overhead": steps["cooling"] / steps["base"] - 1.0}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -659,6 +753,7 @@ def main():
     l1_rho, linf_rho = l1_vs_fp64(s, P0, 20, local)
     l1_64, linf_64 = l1_vs_fp64(s, P0, 20, local, "mixed_fp64")
     suite = None if args.no_workloads or rank != 0 else workload_suite(local, args.serving_requests)
+    next_rows = None if args.no_workloads or rank != 0 else next_rows_suite(local, peak)
 
     if rank != 0:
         return
@@ -687,6 +782,7 @@ def main():
         "clocks": clocks,
         "step_ms_min": min(ms_all), "step_ms_max": max(ms_all),
         "workloads": suite,
+        "next_rows": next_rows,
     }
     print(json.dumps(line))
 

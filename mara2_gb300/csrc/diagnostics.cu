@@ -19,22 +19,30 @@ static CellB<T> cell_b(const void* P, const GridDesc& G)
     return CellB<T>{(const T*) P, G.sP, G.N[0], G.N[1], G.N[2]};
 }
 
-template <typename T>
-__global__ void k_monopole_max(CellB<T> B, GridDesc G, double h, unsigned long long* out)
+// the largest |cell monopole| of the interior zones of a tile, its vertex
+// monopoles formed once (MonoTile)
+template <typename T, int TZ>
+__global__ void __launch_bounds__(256) k_monopole_max_tiled(CellB<T> B, GridDesc G, double h, unsigned long long* out)
 {
-    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-    double m = 0.0;
-    if (ii < G.n[0]) {
-        // cell-centred monopole of an interior zone (full indices)
-        const int i = ii + G.g[0], j = blockIdx.y + G.g[1], k = blockIdx.z + G.g[2];
-        const double M000 = vertex_monopole_at(B, i, j, k, h);
-        const double Mi = M000 + vertex_monopole_at(B, i + 1, j, k, h);
-        const double Mj = M000 + vertex_monopole_at(B, i, j + 1, k, h);
-        const double Mk = M000 + vertex_monopole_at(B, i, j, k + 1, h);
-        m = fabs(1. / 6 * (Mi + Mj + Mk));
+    constexpr int TX = MonoTile<TZ>::TX, TY = MonoTile<TZ>::TY;
+    __shared__ double Mv[TZ + 1][TY + 1][TX + 1];
+    // interior zones ii0.. of the tile; full (guarded) indices g + ii
+    const int ii0 = blockIdx.x * TX, jj0 = blockIdx.y * TY, kk0 = blockIdx.z * TZ;
+    fill_vertex_monopoles<T, TZ>(B, ii0 + G.g[0], jj0 + G.g[1], kk0 + G.g[2], h, Mv);
+    __syncthreads();
+    unsigned long long b = 0;
+    for (int c = threadIdx.x; c < TX * TY * TZ; c += blockDim.x) {
+        const int x = c % TX, y = (c / TX) % TY, z = c / (TX * TY);
+        if (ii0 + x >= G.n[0] || jj0 + y >= G.n[1] || kk0 + z >= G.n[2]) continue;
+        const double M000 = Mv[z][y][x];
+        const double Mi = M000 + Mv[z][y][x + 1];
+        const double Mj = M000 + Mv[z][y + 1][x];
+        const double Mk = M000 + Mv[z + 1][y][x];
+        const double m = fabs(1. / 6 * (Mi + Mj + Mk));
+        unsigned long long bm = (unsigned long long) __double_as_longlong(m);
+        if (!(m >= 0.0)) bm = 0x7ff0000000000000ull;  // NaN reports as +inf
+        b = bm > b ? bm : b;
     }
-    unsigned long long b = (unsigned long long) __double_as_longlong(m);
-    if (!(m >= 0.0)) b = 0x7ff0000000000000ull;  // NaN reports as +inf
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const unsigned long long o = __shfl_down_sync(0xffffffffu, b, off);
@@ -43,20 +51,45 @@ __global__ void k_monopole_max(CellB<T> B, GridDesc G, double h, unsigned long l
     if ((threadIdx.x & 31) == 0) atomicMax(out, b);
 }
 
+template <typename T>
+static void monopole_max_of(const void* P, const GridDesc& G, double h, unsigned long long* out, cudaStream_t s)
+{
+    if (G.n[2] > 1) {
+        using Tl = MonoTile<4>;
+        const dim3 grid((G.n[0] + Tl::TX - 1) / Tl::TX, (G.n[1] + Tl::TY - 1) / Tl::TY, (G.n[2] + 3) / 4);
+        k_monopole_max_tiled<T, 4><<<grid, 256, 0, s>>>(cell_b<T>(P, G), G, h, out);
+    } else {
+        using Tl = MonoTile<1>;
+        const dim3 grid((G.n[0] + Tl::TX - 1) / Tl::TX, (G.n[1] + Tl::TY - 1) / Tl::TY, G.n[2]);
+        k_monopole_max_tiled<T, 1><<<grid, 256, 0, s>>>(cell_b<T>(P, G), G, h, out);
+    }
+}
+
 void launch_monopole_max(const void* P, bool fp32, const GridDesc& G, double h, unsigned long long* out,
                          cudaStream_t s)
 {
-    dim3 grid((G.n[0] + 255) / 256, G.n[1], G.n[2]);
-    if (fp32) k_monopole_max<float><<<grid, 256, 0, s>>>(cell_b<float>(P, G), G, h, out);
-    else k_monopole_max<double><<<grid, 256, 0, s>>>(cell_b<double>(P, G), G, h, out);
+    if (fp32) monopole_max_of<float>(P, G, h, out, s);
+    else monopole_max_of<double>(P, G, h, out, s);
+}
+
+template <typename T>
+static void field_diag_of(const void* P, const GridDesc& G, double h, double* out, cudaStream_t s)
+{
+    if (G.N[2] > 1) {
+        using Tl = MonoTile<4>;
+        const dim3 grid((G.N[0] + Tl::TX - 1) / Tl::TX, (G.N[1] + Tl::TY - 1) / Tl::TY, (G.N[2] + 3) / 4);
+        k_field_diag_tiled<T, 4><<<grid, 256, 0, s>>>(cell_b<T>(P, G), h, out);
+    } else {
+        using Tl = MonoTile<1>;
+        const dim3 grid((G.N[0] + Tl::TX - 1) / Tl::TX, (G.N[1] + Tl::TY - 1) / Tl::TY, G.N[2]);
+        k_field_diag_tiled<T, 1><<<grid, 256, 0, s>>>(cell_b<T>(P, G), h, out);
+    }
 }
 
 void launch_field_diag(const void* P, bool fp32, const GridDesc& G, double h, double* out, cudaStream_t s)
 {
-    const long long total = (long long) G.N[0] * G.N[1] * G.N[2];
-    const unsigned nb = (unsigned) ((total + 255) / 256);
-    if (fp32) k_field_diag<float><<<nb, 256, 0, s>>>(cell_b<float>(P, G), h, out);
-    else k_field_diag<double><<<nb, 256, 0, s>>>(cell_b<double>(P, G), h, out);
+    if (fp32) field_diag_of<float>(P, G, h, out, s);
+    else field_diag_of<double>(P, G, h, out, s);
 }
 
 // interior zone (i, j, k) of the plain path's FP64 primitives with guards

@@ -163,39 +163,67 @@ __device__ __forceinline__ double vertex_monopole_at(const CellB<T>& B, int a, i
     return 0.25 * ((Bx1 - Bx0) + (By1 - By0) + (Bz1 - Bz0)) / h;
 }
 
-// out (N0, N1, N2, 4) AoS, C order: [monopole, current1, current2, current3]
-template <typename T>
-__global__ void __launch_bounds__(256) k_field_diag(CellB<T> B, double h, double* __restrict__ out)
+// Cell monopoles of a tile of cells from its vertex monopoles formed once:
+// a cell's value is 1/6 (3 M000 + M(i+1) + M(j+1) + M(k+1)) of four vertex
+// monopoles (CellCenteredFieldCT.cpp:200-219), and a vertex is shared by the
+// cells around it, so a block first fills the (TX+1) x (TY+1) x (TZ+1) vertex
+// monopoles of its TX x TY x TZ cells into shared memory (the same
+// vertex_monopole_at values, so the same bits as forming them per cell).
+// Tiles: 32 x 8 x 4 cells in 3-D, 32 x 32 x 1 in 2-D; 256 threads.
+template <int TZ> struct MonoTile {
+    static constexpr int TX = 32, TY = TZ > 1 ? 8 : 32;
+    static constexpr int NV = (TX + 1) * (TY + 1) * (TZ + 1);
+};
+
+template <typename T, int TZ>
+__device__ __forceinline__ void fill_vertex_monopoles(const CellB<T>& B, int a0, int b0, int c0, double h,
+                                                      double (*Mv)[MonoTile<TZ>::TY + 1][MonoTile<TZ>::TX + 1])
 {
-    const long long total = (long long) B.N0 * B.N1 * B.N2;
-    const long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-    if (c >= total) return;
-    // AoS cell index, k fastest
-    const int k = (int) (c % B.N2);
-    const int j = (int) ((c / B.N2) % B.N1);
-    const int i = (int) (c / ((long long) B.N2 * B.N1));
-    const double M000 = vertex_monopole_at(B, i, j, k, h);
-    const double Mi = M000 + vertex_monopole_at(B, i + 1, j, k, h);
-    const double Mj = M000 + vertex_monopole_at(B, i, j + 1, k, h);
-    const double Mk = M000 + vertex_monopole_at(B, i, j, k + 1, h);
-    double J[3] = {0.0, 0.0, 0.0};
-    const int r = B.N0 > 1, s = B.N1 > 1, t = B.N2 > 1;
-    const int a = i - r, b = j - s, e = k - t;  // the reference's loop index
-    if (a >= 0 && b >= 0 && e >= 0 && a < B.N0 - 2 * r && b < B.N1 - 2 * s && e < B.N2 - 2 * t) {
-        const double d0B1 = B(a + 2 * r, b, e, 1) - B(a, b, e, 1);
-        const double d0B2 = B(a + 2 * r, b, e, 2) - B(a, b, e, 2);
-        const double d1B2 = B(a, b + 2 * s, e, 2) - B(a, b, e, 2);
-        const double d1B0 = B(a, b + 2 * s, e, 0) - B(a, b, e, 0);
-        const double d2B0 = B(a, b, e + 2 * t, 0) - B(a, b, e, 0);
-        const double d2B1 = B(a, b, e + 2 * t, 1) - B(a, b, e, 1);
-        J[0] = (d1B2 - d2B1) / h / 2;
-        J[1] = (d2B0 - d0B2) / h / 2;
-        J[2] = (d0B1 - d1B0) / h / 2;
+    constexpr int TX = MonoTile<TZ>::TX, TY = MonoTile<TZ>::TY;
+    for (int v = threadIdx.x; v < MonoTile<TZ>::NV; v += blockDim.x) {
+        const int x = v % (TX + 1), y = (v / (TX + 1)) % (TY + 1), z = v / ((TX + 1) * (TY + 1));
+        Mv[z][y][x] = vertex_monopole_at(B, a0 + x, b0 + y, c0 + z, h);
     }
-    out[c * 4 + 0] = 1. / 6 * (Mi + Mj + Mk);
-    out[c * 4 + 1] = J[0];
-    out[c * 4 + 2] = J[1];
-    out[c * 4 + 3] = J[2];
+}
+
+// out (N0, N1, N2, 4) AoS, C order: [monopole, current1, current2, current3]
+template <typename T, int TZ>
+__global__ void __launch_bounds__(256) k_field_diag_tiled(CellB<T> B, double h, double* __restrict__ out)
+{
+    constexpr int TX = MonoTile<TZ>::TX, TY = MonoTile<TZ>::TY;
+    __shared__ double Mv[TZ + 1][TY + 1][TX + 1];
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * TZ;
+    fill_vertex_monopoles<T, TZ>(B, i0, j0, k0, h, Mv);
+    __syncthreads();
+    const int r = B.N0 > 1, s = B.N1 > 1, t = B.N2 > 1;
+    // cells of the tile with k fastest, as the AoS output runs
+    for (int c = threadIdx.x; c < TX * TY * TZ; c += blockDim.x) {
+        const int z = c % TZ, x = (c / TZ) % TX, y = c / (TZ * TX);
+        const int i = i0 + x, j = j0 + y, k = k0 + z;
+        if (i >= B.N0 || j >= B.N1 || k >= B.N2) continue;
+        const double M000 = Mv[z][y][x];
+        const double Mi = M000 + Mv[z][y][x + 1];
+        const double Mj = M000 + Mv[z][y + 1][x];
+        const double Mk = M000 + Mv[z + 1][y][x];
+        double J[3] = {0.0, 0.0, 0.0};
+        const int a = i - r, b = j - s, e = k - t;  // the reference's loop index
+        if (a >= 0 && b >= 0 && e >= 0 && a < B.N0 - 2 * r && b < B.N1 - 2 * s && e < B.N2 - 2 * t) {
+            const double d0B1 = B(a + 2 * r, b, e, 1) - B(a, b, e, 1);
+            const double d0B2 = B(a + 2 * r, b, e, 2) - B(a, b, e, 2);
+            const double d1B2 = B(a, b + 2 * s, e, 2) - B(a, b, e, 2);
+            const double d1B0 = B(a, b + 2 * s, e, 0) - B(a, b, e, 0);
+            const double d2B0 = B(a, b, e + 2 * t, 0) - B(a, b, e, 0);
+            const double d2B1 = B(a, b, e + 2 * t, 1) - B(a, b, e, 1);
+            J[0] = (d1B2 - d2B1) / h / 2;
+            J[1] = (d2B0 - d0B2) / h / 2;
+            J[2] = (d0B1 - d1B0) / h / 2;
+        }
+        const long long o = (((long long) i * B.N1 + j) * B.N2 + k) * 4;
+        out[o + 0] = 1. / 6 * (Mi + Mj + Mk);
+        out[o + 1] = J[0];
+        out[o + 2] = J[1];
+        out[o + 3] = J[2];
+    }
 }
 
 } // namespace mara

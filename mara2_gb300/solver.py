@@ -188,10 +188,16 @@ class Solver:
                 "mara_gpu_volume_diagnostics")
         return dict(zip(diagnostic_names(self.scheme.law, self.scheme.aux), D.tolist()))
 
-    def field_diagnostics(self, mesh_spacing: float = 1.0) -> np.ndarray:
+    def field_diagnostics(self, mesh_spacing: float = 1.0, out: np.ndarray | None = None) -> np.ndarray:
         """[monopole, current1, current2, current3] at every cell of the array
-        with guards, shape full_shape[:3] + (4,) (MHD and RMHD)."""
-        out = np.zeros(tuple(self.scheme.full_shape[:3]) + (4,))
+        with guards, shape full_shape[:3] + (4,) (MHD and RMHD); out, if
+        given, receives them (C-contiguous float64 of that shape; page-locked
+        memory takes the full rate of the host link)."""
+        shape = tuple(self.scheme.full_shape[:3]) + (4,)
+        if out is None:
+            out = np.zeros(shape)
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError(f"field diagnostics buffer must be C-contiguous float64 of shape {shape}")
         N.check(self.lib.mara_gpu_field_diagnostics(self.h, mesh_spacing, out.ctypes.data),
                 "mara_gpu_field_diagnostics")
         return out
