@@ -460,8 +460,9 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
         }
     }
 
-    // 3. divergence, RK combine, store
-    // the rotation's three buffers are distinct arrays
+    // 3. divergence, RK combine, store.  The stage input and output are
+    // distinct buffers; an RK2 last stage writes U0's own buffer, where each
+    // element is read before the value computed from it is written.
     const float* __restrict__ U0h = g.Uh[s];
     const float* __restrict__ U0l = g.Ul[s];
     const float* __restrict__ Uph = g.Uh[src];
