@@ -26,7 +26,8 @@ namespace mara {
 
 struct HGrid {
     float* Uh[3];      // FP32-pair conserved densities, SoA, 5 fields (with an
-    float* Ul[3];      // FP64 accumulator: Uh holds the doubles, Ul unused)
+    float* Ul[3];      // FP64 accumulator: Uh holds the doubles, Ul the same
+                       // values rounded to FP32, which the halo staging reads)
     long long sU;      // field stride (n0 * n1)
     int n0, n1;        // interior zones (n1 = 1 for 1-D)
     int bc;
@@ -283,20 +284,6 @@ __device__ __forceinline__ float ld_state(const float* p)
     else return *p;
 }
 
-// The stage input's FP32 value of field element idx: the high word of the
-// pair (hi = the pair's value rounded to FP32), or the FP64 accumulator
-// rounded to FP32 (ACC64: the array holds doubles).
-template <bool L2ONLY, bool ACC64>
-__device__ __forceinline__ float ld_u32(const float* base, long long idx)
-{
-    if constexpr (ACC64) {
-        const double* p = reinterpret_cast<const double*>(base) + idx;
-        return __double2float_rn(L2ONLY ? __ldcg(p) : *p);
-    } else {
-        return ld_state<L2ONLY>(base + idx);
-    }
-}
-
 // RK weight b of SolutionSchemes.cpp:135-138 in FP64 from its FP32 form
 // (1, 1/2, 1/4 or 2/3)
 __device__ __forceinline__ double rk_b_fp64(float b)
@@ -336,24 +323,28 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     if (stage == 0) { src = s; dst = last ? (s ^ 1) : (s + 1) % 3; }
     else if (stage == 1) { src = (s + 1) % 3; dst = last ? s : (s + 2) % 3; }
     else { src = (s + 2) % 3; dst = s; }
-    const float* __restrict__ Uin = g.Uh[src];
+    // the stage input's FP32 values: the pairs' high words, or the FP64
+    // accumulator's FP32 copy
+    const float* __restrict__ Uin = ACC64 ? g.Ul[src] : g.Uh[src];
     const long long sU = g.sU;
     const int n0 = g.n0, n1 = g.n1;
 
     // L2 prefetch of what the update phase reads per zone besides the
-    // stage input's high word (already staged below): its low word and,
-    // after the first stage, both words of U0
+    // stage input's FP32 values (staged below): the pairs' low words and,
+    // after the first stage, both words of U0; or the FP64 accumulators of
+    // the stage input and, after the first stage, of U0
     {
         const int rows = DIM == 2 ? TY : 1;
         constexpr int W = ACC64 ? 8 : 4;                 // bytes per element
         const int per = (TX * W + 127) / 128;            // 128-byte lines per row segment
-        const int arrays = ACC64 ? (stage == 0 ? 0 : 1) : (stage == 0 ? 1 : 3);
+        const int arrays = ACC64 ? (stage == 0 ? 1 : 2) : (stage == 0 ? 1 : 3);
         const int lines = arrays * 5 * rows * per;
         for (int l = threadIdx.x; l < lines; l += NT) {
             const int seg = l % per, r = (l / per) % rows, q = (l / (per * rows)) % 5, a = l / (per * rows * 5);
             const int y = tr.y0 + r, x = tr.x0 + seg * (128 / W);
             if (y < n1 && x < n0) {
-                const float* base = ACC64 ? g.Uh[s] : a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
+                const float* base = ACC64 ? (a == 0 ? g.Uh[src] : g.Uh[s])
+                                          : a == 0 ? g.Ul[src] : a == 1 ? g.Uh[s] : g.Ul[s];
                 const char* ptr = reinterpret_cast<const char*>(base) + ((long long) q * sU + (long long) y * n0 + x) * W;
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
             }
@@ -381,7 +372,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                     const int lx = c % WX, ly = c / WX;
                     const long long p = base + (long long) ly * n0 + lx;
 #pragma unroll
-                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_u32<L2ONLY, ACC64>(Uin, p + q * sU);
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(Uin + p + q * sU);
                 }
             }
         } else {
@@ -396,7 +387,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                     const int y = DIM == 2 ? bc_image(tr.y0 + ly - G, n1, g.bc, flipy) : 0;
                     const long long o = (long long) y * n0 + x;
 #pragma unroll
-                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_u32<L2ONLY, ACC64>(Uin, q * sU + o);
+                    for (int q = 0; q < 5; ++q) Ur[k][q] = ld_state<L2ONLY>(Uin + q * sU + o);
                     fl[k] = flipx | (flipy << 1);
                 }
             }
@@ -545,6 +536,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                     const double Un = rk_combine_d(u0, L2ONLY ? __ldcg(Upd) : *Upd, f_mul(dt, L), b);
                     reinterpret_cast<double*>(Unh)[q * sU + o] = Un;
                     Unew[q] = __double2float_rn(Un);
+                    Unl[q * sU + o] = Unew[q];   // the FP32 copy the next stage stages
                 } else {
                     // U0 enters only with b < 1 (stage 1 is U + dt L)
                     const df U0 = b == 1.0f ? df{0.0f, 0.0f}

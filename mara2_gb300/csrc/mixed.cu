@@ -663,6 +663,7 @@ __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restri
                 if constexpr (ACC64) {
                     reinterpret_cast<double*>(Uh)[q * G.sU + u] = U[q];
                     hi[q] = __double2float_rn(U[q]);
+                    if (Ul) Ul[q * G.sU + u] = hi[q];   // the fused form's FP32 copy
                 } else {
                     const df d = df_from_double(U[q]);
                     Uh[q * G.sU + u] = d.hi;
@@ -851,6 +852,9 @@ int mixed_create(const MaraGpuConfig* c, const GridDesc& G, MixedState** out, cu
     for (int b = 0; b < 3 && !rc; ++b) {
         if (m->acc64) {
             rc = dev_alloc((void**) &m->Uh[b], sizeof(double) * G.sU * nq, s, bytes);
+            // the fused form also keeps the accumulator rounded to FP32, which
+            // the next stage's halo staging reads (no conversions there)
+            if (!rc && m->fused) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
         } else {
             rc = dev_alloc((void**) &m->Uh[b], sizeof(float) * G.sU * nq, s, bytes);
             if (!rc) rc = dev_alloc((void**) &m->Ul[b], sizeof(float) * G.sU * nq, s, bytes);
