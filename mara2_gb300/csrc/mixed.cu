@@ -448,7 +448,7 @@ __device__ __forceinline__ int recover_acc64(const GridF& G, const double* Un, f
     if constexpr (LAW != LAW_RMHD) {
         float U[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) U[q] = __double2float_rn(Un[q]);
+        for (int q = 0; q < NQ; ++q) U[q] = d2f_rn_ftz(Un[q]);
         return recover_f32<LAW>(G, U, P, code);
     } else {
         return recover_rmhd_fp64(G, Un, P, code, Pprev);
