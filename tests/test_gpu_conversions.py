@@ -27,7 +27,8 @@ def _arguments(n, seed=2027):
         np.float64)
     ends = rng.random(n) * np.where(rng.random(n) < 0.5, 3.4e38 * 1.02, 1.2e-38 * 1.5) * np.where(
         rng.random(n) < 0.5, -1.0, 1.0)
-    bits = rng.integers(0, 2**63, n, dtype=np.int64).view(np.float64) * np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    sign = np.where(rng.random(n) < 0.5, np.uint64(1 << 63), np.uint64(0))
+    bits = (rng.integers(0, 2**63, n, dtype=np.int64).view(np.uint64) | sign).view(np.float64)
     zeros = np.where(rng.random(n) < 0.5, 0.0, -0.0)
     d = np.select([kind == 0, kind == 1, kind == 2, kind == 3, kind == 4], [mag, ties, ends, bits, zeros], mag)
     fb = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32).view(np.float32)
