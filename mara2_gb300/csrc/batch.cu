@@ -157,7 +157,7 @@ __global__ void k_batch_store(HGrid g, int buf, int g0, int g1, int N0, int N1, 
     const long long o = (long long) y * g.n0 + x;
     double U[5];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) U[q] = (double) g.Uh[buf][q * g.sU + o] + (double) g.Ul[buf][q * g.sU + o];
+    for (int q = 0; q < 5; ++q) U[q] = f2d_exact(g.Uh[buf][q * g.sU + o]) + f2d_exact(g.Ul[buf][q * g.sU + o]);
     double P[5];
     hydro_u2p_d(U, gamma - 1.0, P);
     if (fx) P[1] = -P[1];

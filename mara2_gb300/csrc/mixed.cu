@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(CONV_BLOCK) load_kernel(const double* __restri
             for (int q = 0; q < NQ; ++q) {
                 if constexpr (ACC64) {
                     reinterpret_cast<double*>(Uh)[q * G.sU + u] = U[q];
-                    hi[q] = __double2float_rn(U[q]);
+                    hi[q] = d2f_rn_ftz(U[q]);
                     if (Ul) Ul[q * G.sU + u] = hi[q];   // the fused form's FP32 copy
                 } else {
                     const df d = df_from_double(U[q]);
@@ -699,7 +699,7 @@ __device__ __forceinline__ void store_cell(const float* Uh, const float* Ul, lon
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
         if constexpr (ACC64) U[q] = reinterpret_cast<const double*>(Uh)[q * G.sU + u];
-        else U[q] = (double) ld_state<L2ONLY>(Uh + q * G.sU + u) + (double) ld_state<L2ONLY>(Ul + q * G.sU + u);
+        else U[q] = f2d_exact(ld_state<L2ONLY>(Uh + q * G.sU + u)) + f2d_exact(ld_state<L2ONLY>(Ul + q * G.sU + u));
     }
     if constexpr (LAW == LAW_HYDRO) {
         hydro_u2p_d(U, G.gm1_d, P);
@@ -1035,7 +1035,7 @@ struct MixedSrc {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
             if constexpr (ACC64) U[q] = reinterpret_cast<const double*>(Uh)[q * sU + u];
-            else U[q] = (double) Uh[q * sU + u] + (double) Ul[q * sU + u];
+            else U[q] = f2d_exact(Uh[q * sU + u]) + f2d_exact(Ul[q * sU + u]);
         }
         if constexpr (LAW == LAW_HYDRO) {
             hydro_u2p_d(U, gm1, P);

@@ -120,14 +120,60 @@ __device__ __forceinline__ df df_sqrt(df a)
     return fast_two_sum(s, __fmul_rn(d, __fmul_rn(0.5f, rcp_approx(s))));
 }
 
+// ---- FP32 <-> FP64 conversions on the integer pipes -----------------------------
+// The FP64 pipe executes two operations per clock per SM on this GPU, a
+// conversion like an add, and the FP64-accumulator form and the host
+// boundary's FP64 <-> FP32-pair conversions convert per field and zone.
+// These give, bit for bit, the conversion instructions as the FP32
+// translation units compile them (-ftz=true: round to nearest even,
+// subnormal inputs and results as signed zeros), from integer operations.
+
+// float -> double, exact
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned sign = b & 0x80000000u;
+    const unsigned ehi = e == 0xffu ? 0x7ff00000u : (e + 896u) << 20;   // rebias 127 -> 1023
+    return __hiloint2double((int) (e == 0 ? sign : sign | ehi | ((b & 0x7fffffu) >> 3)), (int) (e == 0 ? 0u : b << 29));
+}
+
+// double -> float, round to nearest even; below 2^-126 to signed zero, above
+// the float range to infinity
+__device__ __forceinline__ float d2f_rn_ftz(double d)
+{
+    const unsigned hi = (unsigned) __double2hiint(d), lo = (unsigned) __double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned ed = (hi >> 20) & 0x7ffu;
+    const int e = (int) ed - 896;
+    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);   // the 23 kept mantissa bits
+    const unsigned rest = lo & 0x1fffffffu;                      // the 29 dropped ones
+    const unsigned up = rest > 0x10000000u || (rest == 0x10000000u && (mant & 1u));
+    unsigned bits = ((unsigned) e << 23) + mant + up;            // a carry moves into the exponent
+    if (e <= 0) bits = 0u;
+    if (e >= 255 || bits >= 0x7f800000u) bits = 0x7f800000u;
+    if (ed == 0x7ffu && ((hi & 0xfffffu) | lo)) bits = 0x7fffffffu;   // NaN
+    return __uint_as_float(sign | bits);
+}
+
+// x / 2, exact: the exponent less one while the result stays normal, else the
+// FP64 multiply
+__device__ __forceinline__ double half_exact(double x)
+{
+    const int hi = __double2hiint(x);
+    const unsigned e = ((unsigned) hi >> 20) & 0x7ffu;
+    if (e > 1u && e < 0x7ffu) return __hiloint2double(hi - 0x00100000, __double2loint(x));
+    return __dmul_rn(0.5, x);
+}
+
 __device__ __forceinline__ df df_from_double(double x)
 {
-    const float hi = __double2float_rn(x);
-    const float lo = __double2float_rn(x - (double) hi);
+    const float hi = d2f_rn_ftz(x);
+    const float lo = d2f_rn_ftz(x - f2d_exact(hi));
     return {hi, lo};
 }
 
-__device__ __forceinline__ double df_to_double(df a) { return (double) a.hi + (double) a.lo; }
+__device__ __forceinline__ double df_to_double(df a) { return f2d_exact(a.hi) + f2d_exact(a.lo); }
 
 // U_new = U0 (1 - b) + (U + dt L) b, the RK combine of SolutionSchemes.cpp:
 // 232-235, on FP32 pairs.  b is 1, 1/2, 1/4 or 2/3.
