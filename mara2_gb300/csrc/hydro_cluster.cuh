@@ -62,7 +62,7 @@ struct Cluster1DJob {
 // back to buffer job.buffer of each grid's rotation.  Clusters of one launch
 // may hold grids of different sizes: each CTA uses the zones of its own grid
 // (at most the m the launch's shared memory was sized for).
-template <int RECON, int RIEMANN>
+template <int RECON, int RIEMANN, bool ACC64 = false>
 __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
 {
     namespace cg = cooperative_groups;
@@ -81,6 +81,8 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
     const int z0 = r * m;
     const int mine = max(0, min(m, n - z0));       // zones this CTA owns
 
+    // the state: FP32 pairs (hi, lo), or with ACC64 the FP64 accumulator's
+    // high and low 32-bit halves in the same two arrays
     extern __shared__ float smem[];
     float* Uh = smem;                              // [5][m]
     float* Ul = Uh + 5 * m;
@@ -94,11 +96,22 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
     float* __restrict__ gh = s == 0 ? g.Uh[0] : s == 1 ? g.Uh[1] : g.Uh[2];
     float* __restrict__ gl = s == 0 ? g.Ul[0] : s == 1 ? g.Ul[1] : g.Ul[2];
 
+    auto acc = [](const float* h, const float* l, int k) {
+        return __hiloint2double(__float_as_int(h[k]), __float_as_int(l[k]));
+    };
+    auto set_acc = [](float* h, float* l, int k, double v) {
+        h[k] = __int_as_float(__double2hiint(v));
+        l[k] = __int_as_float(__double2loint(v));
+    };
     for (int i = threadIdx.x; i < mine; i += blockDim.x) {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-            Uh[q * m + i] = gh[q * g.sU + z0 + i];
-            Ul[q * m + i] = gl[q * g.sU + z0 + i];
+            if constexpr (ACC64) {
+                set_acc(Uh, Ul, q * m + i, reinterpret_cast<const double*>(gh)[q * g.sU + z0 + i]);
+            } else {
+                Uh[q * m + i] = gh[q * g.sU + z0 + i];
+                Ul[q * m + i] = gl[q * g.sU + z0 + i];
+            }
         }
     }
     // every CTA follows the same clock: the same doubles from the same inputs
@@ -125,11 +138,12 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
                                                           : (rk == 0 ? 1.f : rk == 1 ? 0.25f : 2.f / 3.f);
             const float omb = 1.f - b;
             float* Ps = Pbuf + par * 5 * W;
-            // 1. primitives of the owned zones (from the high words)
+            // 1. primitives of the owned zones (from the high words, or the
+            //    accumulator rounded to FP32)
             for (int i = threadIdx.x; i < mine; i += blockDim.x) {
                 float U[5], P[5];
 #pragma unroll
-                for (int q = 0; q < 5; ++q) U[q] = Uh[q * m + i];
+                for (int q = 0; q < 5; ++q) U[q] = ACC64 ? d2f_rn_ftz(acc(Uh, Ul, q * m + i)) : Uh[q * m + i];
                 fh_cons(g.gamma, U, P);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) Ps[q * W + G + i] = P[q];
@@ -193,6 +207,15 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
                     const float L = fh_div(Fx[q * (m + 1) + i], Fx[q * (m + 1) + i + 1], g.idx);
+                    if constexpr (ACC64) {
+                        // rk_combine_d as the tile kernels' FP64-accumulator update
+                        const double Upd = acc(Uh, Ul, q * m + i);
+                        if (rk == 0) set_acc(U0h, U0l, q * m + i, Upd);
+                        const double Un = rk_combine_d(rk == 0 ? 0.0 : acc(U0h, U0l, q * m + i), Upd, f_mul(dtf, L), b);
+                        set_acc(Uh, Ul, q * m + i, Un);
+                        Unew[q] = d2f_rn_ftz(Un);
+                        continue;
+                    }
                     const df Up = {Uh[q * m + i], Ul[q * m + i]};
                     df U0 = Up;
                     if (rk == 0) {
@@ -240,8 +263,15 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
     for (int i = threadIdx.x; i < mine; i += blockDim.x) {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-            gh[q * g.sU + z0 + i] = Uh[q * m + i];
-            gl[q * g.sU + z0 + i] = Ul[q * m + i];
+            if constexpr (ACC64) {
+                // the accumulator and its FP32 copy (read by the tile kernels' halo staging)
+                const double v = acc(Uh, Ul, q * m + i);
+                reinterpret_cast<double*>(gh)[q * g.sU + z0 + i] = v;
+                gl[q * g.sU + z0 + i] = d2f_rn_ftz(v);
+            } else {
+                gh[q * g.sU + z0 + i] = Uh[q * m + i];
+                gl[q * g.sU + z0 + i] = Ul[q * m + i];
+            }
         }
     }
     // the clock is published after every CTA's part of the state; the slots
@@ -262,14 +292,14 @@ __global__ void __launch_bounds__(1024) hydro_cluster1d_kernel(Cluster1DJob job)
 // grid of cluster_count clusters of C CTAs, each CTA sized for up to m zones
 // the launch configuration of cluster_count clusters of C CTAs sized for up
 // to m zones each (at[] must outlive the returned configuration)
-template <int RECON, int RIEMANN>
+template <int RECON, int RIEMANN, bool ACC64 = false>
 inline cudaError_t cluster1d_config(int cluster_count, int C, int m, cudaStream_t stream, cudaLaunchAttribute* at,
                                     cudaLaunchConfig_t& lc)
 {
     constexpr int G = HaloOf<RECON>::G;
     const size_t smem = cluster1d_smem_bytes(m, G);
     const int threads = m + 1 < 1024 ? ((m + 1 + 31) / 32) * 32 : 1024;  // one thread per face
-    auto k = hydro_cluster1d_kernel<RECON, RIEMANN>;
+    auto k = hydro_cluster1d_kernel<RECON, RIEMANN, ACC64>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e == cudaSuccess && C > CLUSTER1D_MAX_CTAS)
         e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -289,25 +319,25 @@ inline cudaError_t cluster1d_config(int cluster_count, int C, int m, cudaStream_
 }
 
 // grid of cluster_count clusters of C CTAs, each CTA sized for up to m zones
-template <int RECON, int RIEMANN>
+template <int RECON, int RIEMANN, bool ACC64 = false>
 inline cudaError_t launch_cluster1d(const Cluster1DJob& job, int cluster_count, int C, int m, cudaStream_t stream)
 {
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t lc;
-    const cudaError_t e = cluster1d_config<RECON, RIEMANN>(cluster_count, C, m, stream, at, lc);
+    const cudaError_t e = cluster1d_config<RECON, RIEMANN, ACC64>(cluster_count, C, m, stream, at, lc);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&lc, hydro_cluster1d_kernel<RECON, RIEMANN>, job);
+    return cudaLaunchKernelEx(&lc, hydro_cluster1d_kernel<RECON, RIEMANN, ACC64>, job);
 }
 
 // can the GPU place one cluster of C CTAs sized for m zones?
-template <int RECON, int RIEMANN>
+template <int RECON, int RIEMANN, bool ACC64 = false>
 inline bool cluster1d_fits(int C, int m)
 {
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t lc;
     int n = 0;
-    if (cluster1d_config<RECON, RIEMANN>(1, C, m, nullptr, at, lc) != cudaSuccess ||
-        cudaOccupancyMaxActiveClusters(&n, hydro_cluster1d_kernel<RECON, RIEMANN>, &lc) != cudaSuccess) {
+    if (cluster1d_config<RECON, RIEMANN, ACC64>(1, C, m, nullptr, at, lc) != cudaSuccess ||
+        cudaOccupancyMaxActiveClusters(&n, hydro_cluster1d_kernel<RECON, RIEMANN, ACC64>, &lc) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }

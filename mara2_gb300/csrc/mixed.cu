@@ -1720,11 +1720,11 @@ bool mixed_fused(const MixedState* m) { return m->fused; }
 // ---- small 1-D grids: many steps per launch on one thread-block cluster -------
 bool mixed_cluster_capable(const MixedState* m)
 {
-    return m->fused && !m->acc64 && m->G.n[1] == 1 && m->G.n[2] == 1 &&
+    return m->fused && m->G.n[1] == 1 && m->G.n[2] == 1 &&
            m->G.n[0] <= CLUSTER1D_MAX_CTAS * CLUSTER1D_MAX_ZONES_PER_CTA;
 }
 
-template <int RECON, int RIEMANN>
+template <int RECON, int RIEMANN, bool ACC64>
 static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
 {
     const int n = m->G.n[0];
@@ -1732,7 +1732,7 @@ static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final,
     // fits (a step of 8192 zones: 11.9 us on 8 CTAs, 8.5 us on 16)
     int C = cluster1d_ctas(n);
     const int wide = cluster1d_ctas(n, CLUSTER1D_WIDE_CTAS);
-    if (wide > C && cluster1d_fits<RECON, RIEMANN>(wide, (n + wide - 1) / wide)) C = wide;
+    if (wide > C && cluster1d_fits<RECON, RIEMANN, ACC64>(wide, (n + wide - 1) / wide)) C = wide;
     Cluster1DJob job = {};
     job.grids = m->dgrid;
     job.t = &st->t;
@@ -1747,18 +1747,25 @@ static int cluster_launch(MixedState* m, int nsteps, double cfl, double t_final,
     job.order = m->cfg.rk_order;
     job.nsteps = nsteps;
     job.buffer = host_rot(m);
-    const cudaError_t e = launch_cluster1d<RECON, RIEMANN>(job, 1, C, (n + C - 1) / C, s);
+    const cudaError_t e = launch_cluster1d<RECON, RIEMANN, ACC64>(job, 1, C, (n + C - 1) / C, s);
     return e == cudaSuccess ? MARA_OK : MARA_ERR_CUDA;
 }
 
 int mixed_enqueue_cluster_steps(MixedState* m, int nsteps, double cfl, double t_final, DevStatus* st, cudaStream_t s)
 {
     const bool hllc = m->cfg.riemann == MARA_RIEMANN_HLLC;
+    if (m->acc64) {
+        if (m->cfg.recon == MARA_RECON_PCM)
+            return hllc ? cluster_launch<RECON_PCM, RIEMANN_HLLC, true>(m, nsteps, cfl, t_final, st, s)
+                        : cluster_launch<RECON_PCM, RIEMANN_HLLE, true>(m, nsteps, cfl, t_final, st, s);
+        return hllc ? cluster_launch<RECON_PLM, RIEMANN_HLLC, true>(m, nsteps, cfl, t_final, st, s)
+                    : cluster_launch<RECON_PLM, RIEMANN_HLLE, true>(m, nsteps, cfl, t_final, st, s);
+    }
     if (m->cfg.recon == MARA_RECON_PCM)
-        return hllc ? cluster_launch<RECON_PCM, RIEMANN_HLLC>(m, nsteps, cfl, t_final, st, s)
-                    : cluster_launch<RECON_PCM, RIEMANN_HLLE>(m, nsteps, cfl, t_final, st, s);
-    return hllc ? cluster_launch<RECON_PLM, RIEMANN_HLLC>(m, nsteps, cfl, t_final, st, s)
-                : cluster_launch<RECON_PLM, RIEMANN_HLLE>(m, nsteps, cfl, t_final, st, s);
+        return hllc ? cluster_launch<RECON_PCM, RIEMANN_HLLC, false>(m, nsteps, cfl, t_final, st, s)
+                    : cluster_launch<RECON_PCM, RIEMANN_HLLE, false>(m, nsteps, cfl, t_final, st, s);
+    return hllc ? cluster_launch<RECON_PLM, RIEMANN_HLLC, false>(m, nsteps, cfl, t_final, st, s)
+                : cluster_launch<RECON_PLM, RIEMANN_HLLE, false>(m, nsteps, cfl, t_final, st, s);
 }
 void mixed_set_parity(MixedState* m, int p) { m->rot = p; }
 // the state buffer the device rotation holds (the stream is idle): steps

@@ -147,20 +147,22 @@ CLUSTER_CASES = [(256, "outflow", "plm", "hlle", 2), (1000, "periodic", "plm", "
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp64"])
 @pytest.mark.parametrize("n,bc,recon,riemann,rk", CLUSTER_CASES)
-def test_cluster_run_matches_tile_steps(gpu_lib, n, bc, recon, riemann, rk):
+def test_cluster_run_matches_tile_steps(gpu_lib, n, bc, recon, riemann, rk, precision):
     """A 1-D grid's driver loop on one thread-block cluster (the grid held in
     shared memory across many steps) against the same steps taken one launch
     per stage by the tile kernels: the same clock, step count and bits (the
-    fused kernels share explicitly rounded arithmetic)."""
+    fused kernels share explicitly rounded arithmetic), with either
+    accumulator."""
     s, P = _riemann_1d(n, bc, recon, riemann, rk)
     steps = 40
-    with Solver(s, "mixed") as g:
+    with Solver(s, precision) as g:
         g.upload(P.copy())
         taken = g.run(steps, s.cfl)
         a = g.download()
         t_cluster = g.t
-    with Solver(s, "mixed") as g:
+    with Solver(s, precision) as g:
         g.upload(P.copy())
         t = 0.0
         for _ in range(steps):
