@@ -380,8 +380,9 @@ __device__ __forceinline__ int recover_rmhd_fp64(const GridF& G, const double* U
             // warm start from the zone's primitives of the previous stage
             // (ConsToPrimRMHD::set_starting_prim, ConsToPrimRMHD.cpp:99-108):
             // Z = rho h W^2 and W of the old state are close to the new root
-            const double rho = Pprev[0], pre = Pprev[4];
-            const double V2 = (double) Pprev[1] * Pprev[1] + (double) Pprev[2] * Pprev[2] + (double) Pprev[3] * Pprev[3];
+            const double rho = f2d_exact(Pprev[0]), pre = f2d_exact(Pprev[4]);
+            const double v1 = f2d_exact(Pprev[1]), v2 = f2d_exact(Pprev[2]), v3 = f2d_exact(Pprev[3]);
+            const double V2 = v1 * v1 + v2 * v2 + v3 * v3;
             if (rho > 0.0 && pre > 0.0 && V2 < 1.0) {
                 const double W2 = 1.0 / (1.0 - V2);
                 const double h = 1.0 + pre / rho * (G.inv_gm1_d + 1.0);
@@ -399,7 +400,7 @@ __device__ __forceinline__ int recover_rmhd_fp64(const GridF& G, const double* U
         if (err != ST_OK) err = rm_noble1dw(s, Pd);
         if (err != ST_OK) { *code = err; return ST_INVERSION_FAILURE; }
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) P[q] = (float) Pd[q];
+        for (int q = 0; q < NQ; ++q) P[q] = d2f_rn_ftz(Pd[q]);
         return ST_OK;
     }
 }
