@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel(const __grid_constan
                 const double* dtp;
                 unsigned long long* slot;
                 __device__ float dt() const { return (float) __ldcg(dtp); }
+                __device__ bool proceed() const { return true; }
                 __device__ unsigned long long* cfl() const { return slot; }
             } at{A.dt + tr.grid, A.cflbits + tr.grid};
             const int r = __ldcg(A.rot + tr.grid);
@@ -357,7 +358,7 @@ struct MaraBatch {
 };
 
 typedef void (*TileKernel)(const HGrid*, const TileRef*, const int*, const int*, const double*, int, const int*, int,
-                           int, float, float, int, unsigned long long*, int);
+                           int, float, float, int, unsigned long long*, int, int);
 
 template <int RECON, int RIEMANN>
 static TileKernel pick_1d(int tile)
@@ -422,7 +423,7 @@ static void enqueue_batch_step(MaraBatch* b, int mask)
             tile_dims(b, d + 1, &tx, &ty, &nt);
             TileKernel k = kernel_for(b, d + 1);
             k<<<b->ctas[d], nt, 0, s>>>(b->grids, b->tiles[d], b->ntiles + d, b->rot, b->dt, 1, b->done, 1, rk, bb,
-                                        1.f - bb, last, b->cflbits, 1);
+                                        1.f - bb, last, b->cflbits, 1, 0);
         }
     }
 }

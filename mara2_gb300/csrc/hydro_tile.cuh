@@ -306,7 +306,9 @@ __device__ __forceinline__ double rk_combine_d(double U0, double U, float dtL, f
 //   src: buffer holding the stage input; dst: buffer written; buffer s
 //   holds U0 (read per zone); b, omb = b, 1 - b; on the last stage the
 //   tile's Courant step goes to *at.cfl().  at.dt() and at.cfl() are read
-//   where they are used, so that neither holds registers across the tile.
+//   where they are used, so that neither holds registers across the tile;
+//   at.proceed() (the same in every thread of the CTA) is asked before the
+//   update: false leaves the tile's state as it was.
 //   ACC64: the state arrays (Uh) hold the FP64 accumulator, Ul is unused.
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, bool EARLY = false,
           class At>
@@ -488,6 +490,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
 #pragma unroll
         for (int z = 0; z < NZ; ++z) load(z);
         __syncthreads();
+        if (!at.proceed()) return;
         const float dt = at.dt();
 #pragma unroll
         for (int z = 0; z < NZ; ++z) {
@@ -515,6 +518,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
         // operands loaded zone by zone after the barrier (the kernels that
         // run a tile stage inside a larger loop keep to 64 registers)
         __syncthreads();
+        if (!at.proceed()) return;
         const float dt = at.dt();
         for (int c = threadIdx.x; c < TX * TY; c += NT) {
             const int lx = c % TX, ly = c / TX;
@@ -571,20 +575,34 @@ __global__ void __launch_bounds__(NT, (TileOccupancy<NT, ACC64>::CTAS)) hydro_ti
                                                         const double* __restrict__ dtg, int dt_stride,
                                                         const int* __restrict__ done, int done_stride,
                                                         int stage, float b, float omb, int last,
-                                                        unsigned long long* __restrict__ cfl, int cfl_stride)
+                                                        unsigned long long* __restrict__ cfl, int cfl_stride,
+                                                        int after_begin)
 {
     __shared__ TileSmem<DIM, RECON, TX, TY> sm;
     const int ntiles = *ntiles_p;  // device-resident so a captured graph follows a changing tile list
+    // after_begin: launched as the programmatic dependent of the step-start
+    // kernel (dt, done, the Courant slot's reset), so the tile staging and
+    // the faces, which need none of these, overlap it; the update waits for
+    // it and reads whether the step is taken.  Otherwise a finished grid's
+    // tiles are skipped whole.
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const TileRef tr = tiles[t];
         const HGrid& g = grids[tr.grid];
-        if (done[tr.grid * done_stride]) continue;
+        if (!after_begin && done[tr.grid * done_stride]) continue;
         struct {
             const double* dtp;
             unsigned long long* slot;
+            const int* donep;
+            int wait;
             __device__ float dt() const { return (float) *dtp; }
             __device__ unsigned long long* cfl() const { return slot; }
-        } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride};
+            __device__ bool proceed() const
+            {
+                if (!wait) return true;
+                asm volatile("griddepcontrol.wait;" ::: "memory");
+                return *(volatile const int*) donep == 0;
+            }
+        } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride, done + tr.grid * done_stride, after_begin};
         tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64, true>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
     }
 }

@@ -730,7 +730,16 @@ __global__ void __launch_bounds__(CONV_BLOCK) store_kernel(const float* Uh, cons
     for (int e = threadIdx.x; e < nc * NQ; e += CONV_BLOCK) aos[b0 * NQ + e] = slab[e];
 }
 
-__global__ void k_cfl_reset(unsigned long long* bits) { *bits = (unsigned long long) __double_as_longlong(DBL_MAX); }
+// The step-start kernels let the stage launched after them start at once
+// (programmatic dependent launch): its staging and faces need nothing they
+// write, and it waits for them before its update.
+__device__ __forceinline__ void release_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+__global__ void k_cfl_reset(unsigned long long* bits)
+{
+    release_dependents();
+    *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
+}
 __global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
 // RK1 on the fused path alternates the state buffer; a step that found the
 // loop done (or an error) did no work and keeps it
@@ -754,6 +763,7 @@ __global__ void k_cfl_commit(unsigned long long* bits, const unsigned long long*
 // cannot fail after this point).
 __global__ void k_fused_run_begin(unsigned long long* bits, DevStatus* st, double cfl, double t_final)
 {
+    release_dependents();
     if (st->done) return;
     st->dt_bits = *bits;
     double dt = cfl * __longlong_as_double((long long) st->dt_bits);
@@ -772,6 +782,7 @@ __global__ void k_fused_run_begin(unsigned long long* bits, DevStatus* st, doubl
 // Start of one advance with a given dt on the fused path.
 __global__ void k_fused_advance_begin(unsigned long long* bits, DevStatus* st, double dt)
 {
+    release_dependents();
     st->done = 0;   // an advance with a given dt is always taken
     st->dt = dt;
     *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
@@ -1187,12 +1198,26 @@ template <int DIM, int RECON, int RIEMANN>
 static void tile_launch(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s, int stage, float b, int last)
 {
     constexpr int TX = DIM == 2 ? 32 : 256, TY = DIM == 2 ? 16 : 1, NT = 256;
+    // the first stage follows the step-start kernel as its programmatic
+    // dependent (an eager timing pass launches it plainly)
+    const int after_begin = stage == 0 && !m->timing;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned) m->ctas);
+    lc.blockDim = dim3(NT);
+    lc.stream = s;
+    lc.attrs = at;
+    lc.numAttrs = after_begin ? 1 : 0;
     if (m->acc64)
-        hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT, true><<<m->ctas, NT, 0, s>>>(
-            m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+        cudaLaunchKernelEx(&lc, hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT, true>, (const HGrid*) m->dgrid,
+                           (const TileRef*) m->dtiles, (const int*) m->dntiles, (const int*) m->drot, dt, 0,
+                           (const int*) &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0, after_begin);
     else
-        hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT><<<m->ctas, NT, 0, s>>>(
-            m->dgrid, m->dtiles, m->dntiles, m->drot, dt, 0, &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0);
+        cudaLaunchKernelEx(&lc, hydro_tile_kernel<DIM, RECON, RIEMANN, TX, TY, NT, false>, (const HGrid*) m->dgrid,
+                           (const TileRef*) m->dtiles, (const int*) m->dntiles, (const int*) m->drot, dt, 0,
+                           (const int*) &st->done, 0, stage, b, 1.f - b, last, m->dcfl, 0, after_begin);
 }
 
 template <int DIM>
@@ -1403,6 +1428,7 @@ __global__ void __launch_bounds__(256, 4) host_step_kernel(const __grid_constant
             struct {
                 const HostStepJob* j;
                 __device__ float dt() const { return (float) j->dt; }
+                __device__ bool proceed() const { return true; }
                 __device__ unsigned long long* cfl() const { return j->cfl; }
             } at{&J};
             tile_stage<2, RECON, RIEMANN, 32, 16, 256, true>(sm.t, g, J.tiles[idx], J.r, stage, b, 1.f - b, last, at);
