@@ -46,11 +46,21 @@ template <int RECON> struct SOf { static constexpr int S = RECON == RECON_PCM ? 
 // The face fluxes along one axis of the general form.  AXIS >= 0 is the
 // axis at compile time (no multiplications by the zero components of the
 // normal); AXIS < 0 takes it, and the normal, at run time.
+// The general form's kernels run as a chain of programmatic dependent
+// launches: each waits for the kernel before it (whose writes are then
+// visible) and then lets the next one launch, so a launch's start overlaps
+// its predecessor's last wave.  Outside such a chain both are no-ops.
+__device__ __forceinline__ void pdl_chain()
+{
+    asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int LAW, int RECON, int RIEMANN, int AXIS>
 __global__ void __launch_bounds__(128) flux_f_kernel(const float* __restrict__ P, float* __restrict__ F, GridF G,
                                                      int axis, int lo0, int lo1, int lo2, int nb0, int nb1,
                                                      const int* __restrict__ done, DevStatus* st)
 {
+    pdl_chain();
     if constexpr (AXIS >= 0) axis = AXIS;
     constexpr int NQ = LawInfo<LAW>::NQ;
     constexpr int S = SOf<RECON>::S;
@@ -118,6 +128,7 @@ struct FluxViewF {
 __global__ void __launch_bounds__(128) ct_emf_kernel(FluxViewF V, float* E01, float* E02, float* E12, int M0, int M1,
                                                      int M2, int fx, int fy, int fz)
 {
+    pdl_chain();
     const unsigned L = blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= (unsigned) M0 * (unsigned) M1) return;
     const int i = (int) (L % (unsigned) M0), j = (int) (L / (unsigned) M0), k = blockIdx.y;
@@ -490,6 +501,7 @@ __global__ void __launch_bounds__(128, 8) update_f_kernel(float* __restrict__ Pf
                                                        unsigned long long* cfl)
 {
     constexpr int NQ = LawInfo<LAW>::NQ;
+    pdl_chain();
     if (*done || st->code || st->halt) return;
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = ii < G.n[0];
@@ -737,7 +749,7 @@ __device__ __forceinline__ void release_dependents() { asm volatile("griddepcont
 
 __global__ void k_cfl_reset(unsigned long long* bits)
 {
-    release_dependents();
+    pdl_chain();
     *bits = (unsigned long long) __double_as_longlong(DBL_MAX);
 }
 __global__ void k_cfl_publish(const unsigned long long* bits, DevStatus* st) { st->dt_bits = *bits; }
@@ -752,6 +764,7 @@ __global__ void k_rot_flip(int* rot, const DevStatus* st)
 // t_final or after an error, leaves the previous state's step)
 __global__ void k_cfl_commit(unsigned long long* bits, const unsigned long long* next, const DevStatus* st)
 {
+    pdl_chain();
     if (!st->done && !st->code && !st->halt) *bits = *next;
 }
 
@@ -1090,6 +1103,22 @@ void mixed_volume_diagnostics(MixedState* m, double* partial, int* err, double* 
 }
 
 // ---- general form ------------------------------------------------------------
+// a launch in the general form's chain of programmatic dependents (pdl_chain)
+template <typename... KArgs, typename... Args>
+static void chain_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = grid;
+    lc.blockDim = block;
+    lc.stream = s;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, kernel, std::forward<Args>(args)...);
+}
+
 template <int LAW, int RECON, int RIEMANN>
 static void flux_f_launch(MixedState* m, int axis, const int* done, DevStatus* st, cudaStream_t s)
 {
@@ -1105,12 +1134,12 @@ static void flux_f_launch(MixedState* m, int axis, const int* done, DevStatus* s
     // hydro and MHD fluxes take the axis at compile time; the relativistic
     // law's cost is its quartic, so it keeps one kernel for all axes
     if constexpr (LAW == LAW_RMHD) {
-        flux_f_kernel<LAW, RECON, RIEMANN, -1><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS);
+        chain_launch(flux_f_kernel<LAW, RECON, RIEMANN, -1>, grid, dim3(128), s, MARA_FLUX_ARGS);
     } else {
         switch (axis) {
-            case 0: flux_f_kernel<LAW, RECON, RIEMANN, 0><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
-            case 1: flux_f_kernel<LAW, RECON, RIEMANN, 1><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
-            default: flux_f_kernel<LAW, RECON, RIEMANN, 2><<<grid, 128, 0, s>>>(MARA_FLUX_ARGS); break;
+            case 0: chain_launch(flux_f_kernel<LAW, RECON, RIEMANN, 0>, grid, dim3(128), s, MARA_FLUX_ARGS); break;
+            case 1: chain_launch(flux_f_kernel<LAW, RECON, RIEMANN, 1>, grid, dim3(128), s, MARA_FLUX_ARGS); break;
+            default: chain_launch(flux_f_kernel<LAW, RECON, RIEMANN, 2>, grid, dim3(128), s, MARA_FLUX_ARGS); break;
         }
     }
 #undef MARA_FLUX_ARGS
@@ -1134,6 +1163,7 @@ static void flux_f(MixedState* m, int axis, const int* done, DevStatus* st, cuda
 }
 
 static const float B_TAB[3][3] = {{1.f, 0.f, 0.f}, {1.f, 0.5f, 0.f}, {1.f, 0.25f, 2.f / 3.f}};
+
 
 static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStream_t s)
 {
@@ -1160,8 +1190,8 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
         if (m->E[0]) {
             dim3 eg((unsigned) (((long long) V.M0 * V.M1 + 127) / 128), m->G.N[2] + 1);
             timed(m, s, [&] {
-                ct_emf_kernel<<<eg, 128, 0, s>>>(V, m->E[0], m->E[1], m->E[2], V.M0, V.M1, m->G.N[2] + 1,
-                                                 m->G.n[0] > 1, m->G.n[1] > 1, m->G.n[2] > 1);
+                chain_launch(ct_emf_kernel, eg, dim3(128), s, V, m->E[0], m->E[1], m->E[2], V.M0, V.M1,
+                             m->G.N[2] + 1, (int) (m->G.n[0] > 1), (int) (m->G.n[1] > 1), (int) (m->G.n[2] > 1));
             });
         }
         const float b = B_TAB[order - 1][rk];
@@ -1169,28 +1199,29 @@ static void general_step(MixedState* m, const double* dt, DevStatus* st, cudaStr
         const int dst = rk == order - 1 ? sb : tb;
         const bool last = rk == order - 1;
         // the last stage also reduces the new state's Courant step
-        if (last) k_cfl_reset<<<1, 1, 0, s>>>(m->dcfl_next);
+        if (last) chain_launch(k_cfl_reset, dim3(1), dim3(1), s, m->dcfl_next);
         unsigned long long* cfl = last ? m->dcfl_next : nullptr;
         dim3 grid((m->G.n[0] + 127) / 128, m->G.n[1], m->G.n[2]);
         timed(m, s, [&] {
 #define MARA_UPDATE_ARGS m->Pf, m->Uh[sb], m->Ul[sb], m->Uh[src], m->Ul[src], m->Uh[dst], m->Ul[dst], V, m->GF, dt, b, 1.f - b, done, st, cfl
             if (m->acc64) {
                 switch (m->cfg.law) {
-                    case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                    case MARA_LAW_MHD: update_f_kernel<LAW_MHD, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                    default: update_f_kernel<LAW_RMHD, true><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_HYDRO: chain_launch(update_f_kernel<LAW_HYDRO, true>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_MHD: chain_launch(update_f_kernel<LAW_MHD, true>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
+                    default: chain_launch(update_f_kernel<LAW_RMHD, true>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
                 }
             } else {
                 switch (m->cfg.law) {
-                    case MARA_LAW_HYDRO: update_f_kernel<LAW_HYDRO, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                    case MARA_LAW_MHD: update_f_kernel<LAW_MHD, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
-                    default: update_f_kernel<LAW_RMHD, false><<<grid, 128, 0, s>>>(MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_HYDRO: chain_launch(update_f_kernel<LAW_HYDRO, false>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
+                    case MARA_LAW_MHD: chain_launch(update_f_kernel<LAW_MHD, false>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
+                    default: chain_launch(update_f_kernel<LAW_RMHD, false>, grid, dim3(128), s, MARA_UPDATE_ARGS); break;
                 }
             }
 #undef MARA_UPDATE_ARGS
         });
     }
-    k_cfl_commit<<<1, 1, 0, s>>>(m->dcfl, m->dcfl_next, st);
+    chain_launch(k_cfl_commit, dim3(1), dim3(1), s, m->dcfl, (const unsigned long long*) m->dcfl_next,
+                 (const DevStatus*) st);
 }
 
 // ---- fused hydro tiles ------------------------------------------------------
