@@ -43,7 +43,9 @@ typedef struct MaraBatchConfig {
     int riemann;               /* MARA_RIEMANN_*                            */
     int rk_order;              /* 1, 2, 3                                   */
     int tile_1d;               /* zones per 1-D tile: 128, 256, 512, 0=auto */
-    int tile_2d;               /* 2-D tile: 0=auto, 1=32x8, 2=32x16, 3=64x8 */
+    int tile_2d;               /* 2-D tile: 0=auto, 1=32x8, 2=32x16, 3=64x8,
+                                  4=32x16 one face per thread (PLM faces
+                                  otherwise go in runs along their normal) */
     int lockstep_1d;           /* 1: small 1-D grids step with the tile lists
                                   (0: on thread-block clusters, see below)  */
     int persistent;            /* 1: one cooperative launch per batch step

@@ -27,7 +27,7 @@ from . import _native as N
 from .scheme import Scheme
 
 MARA_ERR_NO_ROOM = 36
-TILE_2D = {1: "32x8", 2: "32x16", 3: "64x8"}
+TILE_2D = {1: "32x8", 2: "32x16", 3: "64x8", 4: "32x16-oneface"}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotune.json")
 
 
@@ -248,7 +248,8 @@ def autotune(device: int = 0, sample: int = 48, steps: int = 40, force: bool = F
     Riemann workload (grids of the stream's size distribution) and cache the
     fastest: the 1-D tile (128 / 256 / 512 zones, 1-D grids in the tile
     lists), then for the 2-D grids the launch form - per-stage launches with
-    each 2-D tile shape (32x8, 32x16, 64x8), or the persistent cooperative
+    each 2-D tile shape (32x8, 32x16, 64x8; PLM faces in runs along their
+    normal) and 32x16 with one face per thread, or the persistent cooperative
     launch with each tile shape it supports (32x8, 32x16) and 2, 3 or 4 CTAs
     per SM."""
     if not force and os.path.exists(CACHE):
@@ -282,7 +283,7 @@ def autotune(device: int = 0, sample: int = 48, steps: int = 40, force: bool = F
     best["tile_1d"] = min(timing1, key=timing1.get)
     best["timing_1d_ms"] = {str(k): v * 1e3 for k, v in timing1.items()}
     sel2 = [(s, P) for s, P in grids if s.dims == 2]
-    cands = [("stage", t2, 0) for t2 in (1, 2, 3)] + [("persistent", t2, c) for t2 in (1, 2) for c in (2, 3, 4)]
+    cands = [("stage", t2, 0) for t2 in (1, 2, 3, 4)] + [("persistent", t2, c) for t2 in (1, 2) for c in (2, 3, 4)]
     timing = {}
     for form, t2, ctas in cands:
         timing[(form, t2, ctas)] = time_batch(sel2, tile_2d=t2, persistent=form == "persistent", ctas_per_sm=ctas)

@@ -288,8 +288,8 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel(const __grid_constan
                 }
             }
             if constexpr ((MASK & 2) != 0)
-                tile_stage<2, RECON, RIEMANN, 32, TY2, 256, false>(sm.s2, A.grids[tr.grid], tr, r, rk, b, 1.f - b,
-                                                                   last, at);
+                tile_stage<2, RECON, RIEMANN, 32, TY2, 256, false, false, false, true>(sm.s2, A.grids[tr.grid], tr, r,
+                                                                                    rk, b, 1.f - b, last, at);
         }
         // the last stage's Courant reductions are read by the next launch
         if (!last && !grid_barrier(A)) return;
@@ -376,6 +376,7 @@ static TileKernel pick_2d(int tile)
     switch (tile) {
         case 1: return hydro_tile_kernel<2, RECON, RIEMANN, 32, 8, 256>;
         case 3: return hydro_tile_kernel<2, RECON, RIEMANN, 64, 8, 256>;
+        case 4: return hydro_tile_kernel<2, RECON, RIEMANN, 32, 16, 256, false, true>;
         default: return hydro_tile_kernel<2, RECON, RIEMANN, 32, 16, 256>;
     }
 }
@@ -606,7 +607,7 @@ int mara_batch_create(const MaraBatchConfig* c, MaraBatch** out)
     b->cfg = *c;
     b->nslots = c->max_grids;
     b->tile1 = (c->tile_1d == 128 || c->tile_1d == 256 || c->tile_1d == 512) ? c->tile_1d : 256;
-    b->tile2 = (c->tile_2d >= 1 && c->tile_2d <= 3) ? c->tile_2d : 2;
+    b->tile2 = (c->tile_2d >= 1 && c->tile_2d <= 4) ? c->tile_2d : 2;
     b->clusters = !c->lockstep_1d;
     for (int k = 0; k < CLUSTER_BUCKETS; ++k) b->cl_steps[k] = 256;
     b->slots.resize(b->nslots);

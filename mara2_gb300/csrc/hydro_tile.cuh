@@ -264,15 +264,77 @@ __device__ __forceinline__ void block_min_to(unsigned long long* dst, float v)
     if ((threadIdx.x & 31) == 0 && b != ~0ull) atomicMin(dst, b);
 }
 
-// shared memory of one tile stage
+// The faces of a 2-D PLM tile are computed in runs: a run is RL consecutive
+// faces along their normal in one row (x faces) or column (y faces), RL
+// chosen so that the tile's runs about fill the block once, and a run forms
+// each zone's limited slope once for the right state of the face on the
+// zone's left and the left state of the face on its right: (RL + 1) / (2 RL)
+// of the minmods of faces taken one at a time, with the same bits.
+template <int DIM, int RECON, int TX, int TY, int NT>
+struct FaceRuns {
+    static constexpr bool ON = DIM == 2 && RECON == RECON_PLM;
+    static constexpr int NF = (TX + 1) * TY + TX * (TY + 1);
+    static constexpr int RL0 = NF / NT < 1 ? 1 : NF / NT;
+    static constexpr int RL = RL0 > TY + 1 ? TY + 1 : RL0;
+    static constexpr int SX = (TX + 1) / RL, SY = (TY + 1) / RL;   // runs per row / per column
+    static constexpr int LX = (TX + 1) / SX, LY = (TY + 1) / SY;   // faces per run but the last
+    static constexpr int NXR = SX * TY, NR = NXR + SY * TX;
+};
+
+// shared memory of one tile stage; the primitives' rows have an odd pitch
+// under face runs, so that the x runs a warp reads meet in no bank
 template <int DIM, int RECON, int TX, int TY>
 struct TileSmem {
     static constexpr int G = HaloOf<RECON>::G;
-    float Ps[5][DIM == 2 ? TY + 2 * G : 1][TX + 2 * G];
-    float Uc[5][TY][TX];   // the stage input's high words of the tile's zones
+    static constexpr int PAD = (DIM == 2 && RECON == RECON_PLM && (TX + 2 * G) % 2 == 0) ? 1 : 0;
+    float Ps[5][DIM == 2 ? TY + 2 * G : 1][TX + 2 * G + PAD];
+    float Uc[5][TY][TX];   // the stage input's high words of the tile's zones (EARLY)
     float Fx[5][TY][TX + 1];
     float Fy[5][DIM == 2 ? TY + 1 : 1][DIM == 2 ? TX : 1];
 };
+
+// PLM fluxes of the faces a .. e-1 of row `line` (AXIS 0: x faces, face f
+// left of tile zone f) or column `line` (AXIS 1: y faces, face f below tile
+// row f) of a tile, in order.  Each zone's limited slope s is formed once:
+// fma(-1/2, s, u) is the right state of the face on the zone's left and
+// fma(1/2, s, u) the left state of the face on its right, the values
+// recon_pair forms one face at a time.
+template <int RIEMANN, int AXIS, int DIM, int RECON, int TX, int TY>
+__device__ __forceinline__ void plm_face_run(TileSmem<DIM, RECON, TX, TY>& sm, int line, int a, int e, float theta,
+                                             float gamma)
+{
+    constexpr int G = HaloOf<RECON>::G;
+    // primitive k of the line's stencil (k = f + 1 and f + 2 straddle face f)
+    auto ps = [&](int q, int k) -> float { return AXIS == 0 ? sm.Ps[q][line + G][k] : sm.Ps[q][k][line + G]; };
+    float u1[5], u2[5], PL[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const float u0 = ps(q, a);
+        u1[q] = ps(q, a + 1);
+        u2[q] = ps(q, a + 2);
+        PL[q] = f_fma(0.5f, fh_minmod(theta, u0, u1[q], u2[q]), u1[q]);
+    }
+#pragma unroll 1
+    for (int f = a; f < e; ++f) {
+        float PR[5], NL[5], Fh[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const float u3 = ps(q, f + 3);
+            const float s = fh_minmod(theta, u1[q], u2[q], u3);
+            PR[q] = f_fma(-0.5f, s, u2[q]);
+            NL[q] = f_fma(0.5f, s, u2[q]);
+            u1[q] = u2[q];
+            u2[q] = u3;
+        }
+        hydro_face_flux<RIEMANN, AXIS>(gamma, PL, PR, Fh);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            if (AXIS == 0) sm.Fx[q][line][f] = Fh[q];
+            else sm.Fy[q][f][line] = Fh[q];
+            PL[q] = NL[q];
+        }
+    }
+}
 
 // a load of the state: through L1 in the stage kernels (nothing a stage
 // reads changes during its launch), from L2 where CTAs of one launch read
@@ -309,8 +371,13 @@ __device__ __forceinline__ double rk_combine_d(double U0, double U, float dtL, f
 //   where they are used, so that neither holds registers across the tile;
 //   at.proceed() (the same in every thread of the CTA) is asked before the
 //   update: false leaves the tile's state as it was.
-//   ACC64: the state arrays (Uh) hold the FP64 accumulator, Ul is unused.
+//   ACC64: the state arrays Uh hold the FP64 accumulator, Ul its FP32 copy.
+//   EARLY: the FP32-pair update's operands loaded before the barrier that
+//   ends the face phase (registers for 3 CTAs of 256 threads per SM).
+//   RUNS: a 2-D PLM tile's faces in runs (FaceRuns), else one face per
+//   thread at a time.
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, bool EARLY = false,
+          bool RUNS = false,
           class At>
 __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, const HGrid& g, const TileRef& tr,
                                            int s, int stage, float b, float omb, int last, const At& at)
@@ -420,8 +487,25 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     __syncthreads();
 
     const float theta = g.plm_theta, gamma = g.gamma;
-    // 2. x faces and y faces in one balanced loop (face fx sits left of
-    //    tile zone fx, face fy below tile row fy)
+    // 2. x faces and y faces (face fx sits left of tile zone fx, face fy
+    //    below tile row fy): in runs along their normals (2-D PLM), else one
+    //    face per thread in one balanced loop
+    using Runs = FaceRuns<DIM, RECON, TX, TY, NT>;
+    if constexpr (RUNS && Runs::ON) {
+        for (int r = threadIdx.x; r < Runs::NR; r += NT) {
+            if (r < Runs::NXR) {
+                // a warp's x runs: rows side by side, runs of a row adjacent
+                const int j = r % Runs::SX, fy = r / Runs::SX;
+                const int a = j * Runs::LX, e = j == Runs::SX - 1 ? TX + 1 : a + Runs::LX;
+                plm_face_run<RIEMANN, 0>(sm, fy, a, e, theta, gamma);
+            } else {
+                const int h = r - Runs::NXR;
+                const int fx = h % TX, j = h / TX;
+                const int a = j * Runs::LY, e = j == Runs::SY - 1 ? TY + 1 : a + Runs::LY;
+                plm_face_run<RIEMANN, 1>(sm, fx, a, e, theta, gamma);
+            }
+        }
+    } else
     for (int f = threadIdx.x; f < FXN + (DIM == 2 ? FYN : 0); f += NT) {
         float PL[5], PR[5], Fh[5];
         if (f < FXN) {
@@ -558,25 +642,31 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     if (last) block_min_to(at.cfl(), zdt);
 }
 
-// Resident CTAs per SM the stage kernels are compiled for: the FP32-pair
-// update holds its zones' operands across the face phase's barrier, which
-// wants up to 85 registers a thread (3 CTAs of 256 threads per SM: 3 % faster
-// on KH 1024^2 than 4 CTAs at 64 registers with spills, or than the operands
-// loaded after the barrier); the FP64-accumulator form stays at 64 registers
-// and 4 CTAs.
-template <int NT, bool ACC64> struct TileOccupancy { static constexpr int CTAS = ACC64 ? 1024 / NT : 768 / NT; };
+// The stage kernel's form for a tile shape: 2-D PLM tiles take their faces
+// in runs at 4 CTAs of 256 threads per SM (64 registers a thread, no
+// spills; KH 1024^2 with FP32 pairs 0.0880 ms a step against 0.0957 ms at 3
+// CTAs and 0.0903 ms for one face per thread with the early operand loads).
+// The other FP32-pair tiles keep one face per thread with the early loads at
+// 3 CTAs (80 registers), 11 % faster than 4 CTAs without them on 1-D tiles
+// of 256 zones; the FP64-accumulator form has no early loads and runs at 4
+// CTAs.  ONEFACE keeps a 2-D PLM tile at one face per thread with the
+// early loads (the batch's 32 x 16 tiles on small grids, where it measured
+// faster).
+template <int DIM, int RECON, int TX, int TY, int NT, bool ACC64, bool ONEFACE = false> struct TileForm {
+    static constexpr bool RUNS = FaceRuns<DIM, RECON, TX, TY, NT>::ON && !ONEFACE;
+    static constexpr bool EARLY = !RUNS && !ACC64;
+    static constexpr int CTAS = EARLY ? 768 / NT : 1024 / NT;
+};
 
 // One RK stage over a list of tiles (persistent: CTAs stride over tiles).
-template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool ACC64 = false>
-__global__ void __launch_bounds__(NT, (TileOccupancy<NT, ACC64>::CTAS)) hydro_tile_kernel(const HGrid* __restrict__ grids,
-                                                        const TileRef* __restrict__ tiles,
-                                                        const int* __restrict__ ntiles_p,
-                                                        const int* __restrict__ rot,  // per grid: state buffer s
-                                                        const double* __restrict__ dtg, int dt_stride,
-                                                        const int* __restrict__ done, int done_stride,
-                                                        int stage, float b, float omb, int last,
-                                                        unsigned long long* __restrict__ cfl, int cfl_stride,
-                                                        int after_begin)
+template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool ACC64 = false, bool ONEFACE = false>
+__global__ void __launch_bounds__(NT, (TileForm<DIM, RECON, TX, TY, NT, ACC64, ONEFACE>::CTAS))
+    hydro_tile_kernel(const HGrid* __restrict__ grids, const TileRef* __restrict__ tiles,
+                      const int* __restrict__ ntiles_p,
+                      const int* __restrict__ rot,  // per grid: state buffer s
+                      const double* __restrict__ dtg, int dt_stride, const int* __restrict__ done, int done_stride,
+                      int stage, float b, float omb, int last, unsigned long long* __restrict__ cfl, int cfl_stride,
+                      int after_begin)
 {
     __shared__ TileSmem<DIM, RECON, TX, TY> sm;
     const int ntiles = *ntiles_p;  // device-resident so a captured graph follows a changing tile list
@@ -603,7 +693,9 @@ __global__ void __launch_bounds__(NT, (TileOccupancy<NT, ACC64>::CTAS)) hydro_ti
                 return *(volatile const int*) donep == 0;
             }
         } at{dtg + tr.grid * dt_stride, cfl + tr.grid * cfl_stride, done + tr.grid * done_stride, after_begin};
-        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64, true>(sm, g, tr, rot[tr.grid], stage, b, omb, last, at);
+        using Form = TileForm<DIM, RECON, TX, TY, NT, ACC64, ONEFACE>;
+        tile_stage<DIM, RECON, RIEMANN, TX, TY, NT, false, ACC64, Form::EARLY, Form::RUNS>(sm, g, tr, rot[tr.grid], stage, b,
+                                                                                    omb, last, at);
     }
 }
 

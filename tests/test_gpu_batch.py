@@ -204,6 +204,31 @@ def test_persistent_launch_matches_per_stage_launches(gpu_lib, recon, riemann, r
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("riemann,rk", [("hllc", 2), ("hlle", 3)])
+def test_tile_shapes_and_face_forms_agree(gpu_lib, riemann, rk):
+    """Every 2-D tile choice of the per-stage launches (32x8, 32x16 and 64x8
+    with the PLM faces in runs along their normal, 32x16 with one face per
+    thread) and the persistent launch with runs: the same clock, step count
+    and bits."""
+    reqs = W.riemann_stream(24, rate=1e6, seed=23, n1=(64, 2048), n2=(40, 200))
+    built = []
+    for r in reqs[:12]:
+        s, P = W.riemann_initial(r)
+        s = s.with_(recon="plm", riemann=riemann, rk_order=rk, t_final=0.01, guard=2)
+        built.append((s, W.apply_bc_numpy(s, P)))
+    assert any(s.dims == 2 for s, _ in built)
+    kw = dict(recon="plm", riemann=riemann, rk_order=rk, tile_1d=256, lockstep_1d=True)
+    ref = _run_batch(built, tile_2d=4, **kw)
+    for form in ({"tile_2d": 1}, {"tile_2d": 2}, {"tile_2d": 3}, {"tile_2d": 2, "persistent": True}):
+        got = _run_batch(built, **form, **kw)
+        for k, (s, _) in enumerate(built):
+            Pa, ta, na = ref[k]
+            Pb, tb, nb = got[k]
+            assert na == nb and ta == tb, (form, k, na, nb)
+            assert np.array_equal(Pa[s.interior()].view(np.uint64), Pb[s.interior()].view(np.uint64)), (form, k)
+
+
+@pytest.mark.gpu
 def test_persistent_serving_alone_equals_mix(gpu_lib):
     """Continuous batching on the persistent form: each request's result is
     the same alone and in the mix (small 1-D grids on their clusters)."""
