@@ -281,8 +281,9 @@ struct FaceRuns {
     static constexpr int NXR = SX * TY, NR = NXR + SY * TX;
 };
 
-// shared memory of one tile stage; the primitives' rows have an odd pitch
-// under face runs, so that the x runs a warp reads meet in no bank
+// shared memory of one tile stage; under face runs the primitives' rows
+// have an odd pitch, which spreads the x runs a warp reads over the banks
+// (at most 2-way conflicts for a 32 x 16 tile)
 template <int DIM, int RECON, int TX, int TY>
 struct TileSmem {
     static constexpr int G = HaloOf<RECON>::G;
@@ -494,8 +495,10 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     if constexpr (RUNS && Runs::ON) {
         for (int r = threadIdx.x; r < Runs::NR; r += NT) {
             if (r < Runs::NXR) {
-                // a warp's x runs: rows side by side, runs of a row adjacent
-                const int j = r % Runs::SX, fy = r / Runs::SX;
+                // the runs of one index in every row side by side, so that the
+                // longer last runs of the rows share warps (a 32 x 16 tile: 17
+                // warp iterations over the x faces instead of 20)
+                const int j = r / TY, fy = r % TY;
                 const int a = j * Runs::LX, e = j == Runs::SX - 1 ? TX + 1 : a + Runs::LX;
                 plm_face_run<RIEMANN, 0>(sm, fy, a, e, theta, gamma);
             } else {
