@@ -289,7 +289,7 @@ struct TileSmem {
     static constexpr int G = HaloOf<RECON>::G;
     static constexpr int PAD = (DIM == 2 && RECON == RECON_PLM && (TX + 2 * G) % 2 == 0) ? 1 : 0;
     float Ps[5][DIM == 2 ? TY + 2 * G : 1][TX + 2 * G + PAD];
-    float Uc[5][TY][TX];   // the stage input's high words of the tile's zones (EARLY)
+    float Uc[5][TY][TX];   // the stage input's high words of the tile's zones (EARLY or RUNS)
     float Fx[5][TY][TX + 1];
     float Fy[5][DIM == 2 ? TY + 1 : 1][DIM == 2 ? TX : 1];
 };
@@ -469,7 +469,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                 const int lx = c % WX, ly = c / WX;
                 if (fl[k] & 1) Ur[k][1] = -Ur[k][1];
                 if (fl[k] & 2) Ur[k][2] = -Ur[k][2];
-                if constexpr (EARLY && !ACC64) {
+                if constexpr ((EARLY || RUNS) && !ACC64) {
                     // a zone of the tile itself: keep its conserved high words
                     // for the update (halo zones of a tile never are)
                     const int zx = lx - G, zy = DIM == 2 ? ly - G : 0;
@@ -632,7 +632,10 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
                     // U0 enters only with b < 1 (stage 1 is U + dt L)
                     const df U0 = b == 1.0f ? df{0.0f, 0.0f}
                                             : df{ld_state<L2ONLY>(U0h + q * sU + o), ld_state<L2ONLY>(U0l + q * sU + o)};
-                    const df Up = {ld_state<L2ONLY>(Uph + q * sU + o), ld_state<L2ONLY>(Upl + q * sU + o)};
+                    // the stage input's high words: kept in shared memory by the
+                    // staging under face runs
+                    const df Up = {RUNS ? sm.Uc[q][ly][lx] : ld_state<L2ONLY>(Uph + q * sU + o),
+                                   ld_state<L2ONLY>(Upl + q * sU + o)};
                     const df Un = rk_combine(U0, Up, f_mul(dt, L), b, omb);
                     Unh[q * sU + o] = Un.hi;
                     Unl[q * sU + o] = Un.lo;
