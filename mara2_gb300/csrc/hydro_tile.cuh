@@ -376,7 +376,8 @@ __device__ __forceinline__ double rk_combine_d(double U0, double U, float dtL, f
 //   EARLY: the FP32-pair update's operands loaded before the barrier that
 //   ends the face phase (registers for 3 CTAs of 256 threads per SM).
 //   RUNS: a 2-D PLM tile's faces in runs (FaceRuns), else one face per
-//   thread at a time.
+//   thread at a time; and the tile's stage-input high words kept in shared
+//   memory by the staging for the update.
 template <int DIM, int RECON, int RIEMANN, int TX, int TY, int NT, bool L2ONLY, bool ACC64 = false, bool EARLY = false,
           bool RUNS = false,
           class At>
