@@ -279,6 +279,19 @@ struct FaceRuns {
     static constexpr int SX = (TX + 1) / RL, SY = (TY + 1) / RL;   // runs per row / per column
     static constexpr int LX = (TX + 1) / SX, LY = (TY + 1) / SY;   // faces per run but the last
     static constexpr int NXR = SX * TY, NR = NXR + SY * TX;
+    // the runs of a row (n = TX + 1 faces, S runs of L) or a column cover
+    // its faces once each, in order, with no run empty
+    static constexpr bool covers(int n, int S, int L)
+    {
+        int next = 0;
+        for (int j = 0; j < S; ++j) {
+            const int a = j * L, e = j == S - 1 ? n : a + L;
+            if (a != next || e <= a) return false;
+            next = e;
+        }
+        return next == n;
+    }
+    static constexpr bool VALID = !ON || (covers(TX + 1, SX, LX) && covers(TY + 1, SY, LY));
 };
 
 // shared memory of one tile stage; under face runs the primitives' rows
@@ -493,6 +506,7 @@ __device__ __forceinline__ void tile_stage(TileSmem<DIM, RECON, TX, TY>& sm, con
     //    below tile row fy): in runs along their normals (2-D PLM), else one
     //    face per thread in one balanced loop
     using Runs = FaceRuns<DIM, RECON, TX, TY, NT>;
+    static_assert(Runs::VALID, "face runs must cover every face of a tile line once");
     if constexpr (RUNS && Runs::ON) {
         for (int r = threadIdx.x; r < Runs::NR; r += NT) {
             if (r < Runs::NXR) {
