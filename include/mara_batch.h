@@ -31,7 +31,10 @@ enum {
 };
 
 enum {
-    MARA_TILE_AUTO = 0      /* pick tile shapes with the autotuner's table */
+    MARA_TILE_AUTO = 0      /* the default tile shape (1-D: 256 zones, 2-D:
+                               32x16); the autotuner (mara2_gb300.batch.
+                               autotune) measures the others on the request
+                               mix and its caller passes the fastest */
 };
 
 typedef struct MaraBatchConfig {
@@ -42,8 +45,8 @@ typedef struct MaraBatchConfig {
     int recon;                 /* MARA_RECON_PCM or MARA_RECON_PLM          */
     int riemann;               /* MARA_RIEMANN_*                            */
     int rk_order;              /* 1, 2, 3                                   */
-    int tile_1d;               /* zones per 1-D tile: 128, 256, 512, 0=auto */
-    int tile_2d;               /* 2-D tile: 0=auto, 1=32x8, 2=32x16, 3=64x8,
+    int tile_1d;               /* zones per 1-D tile: 128, 256, 512, 0=256  */
+    int tile_2d;               /* 2-D tile: 0=32x16, 1=32x8, 2=32x16, 3=64x8,
                                   4=32x16 one face per thread (PLM faces
                                   otherwise go in runs along their normal) */
     int lockstep_1d;           /* 1: small 1-D grids step with the tile lists
@@ -99,7 +102,7 @@ int mara_batch_retire(MaraBatch* b, int slot, double* P_aos, double* t, int64_t*
 
 int mara_batch_stats(MaraBatch* b, MaraBatchStats* stats);
 
-/* The tile shapes in use (after autotuning). */
+/* The tile shapes in use (as configured, or the defaults). */
 int mara_batch_tiles(MaraBatch* b, int* tile_1d, int* tile_2d);
 
 /* The launch form in use: *persistent = 1 with *ctas CTAs in the one
